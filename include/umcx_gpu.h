@@ -1,0 +1,173 @@
+/*
+ * umcx_gpu.h - C ABI of the GB300 photon-transport library (libumcx_gb300.so).
+ *
+ * Plain C types only: pointers, sizes, PODs.  Every entry point returns an int status (UMCX_OK = 0) and
+ * never lets a C++ exception cross the boundary; the message of the last failure on a context is returned by
+ * umcx_last_error().
+ *
+ * Reference interfaces replaced (fangq/umcx, src/umcx.cpp):
+ *   MCX_run_cmd / MCX_run_json            src/umcx.cpp:850-856  (same symbols, same argv / JSON semantics)
+ *   MCX_kernel<isreflect,issavedet>()     src/umcx.cpp:722-781  (-> umcx_gpu_forward*)
+ *   MCX_param                              src/umcx.cpp:95-99    (-> umcx_sim)
+ *   MCX_medium                             src/umcx.cpp:89-93    (-> float[4] {mua, mus, g, n} per label)
+ *   MCX_volume<int> labels + DET_MASK      src/umcx.cpp:102-146, 35-36 (-> uint8 labels, bit 7 = detector voxel)
+ *   MCX_volume<float> output               src/umcx.cpp:102-146  (-> float fluence [gate][x][y][z])
+ *   MCX_detect                             src/umcx.cpp:149-185  (-> float detp [saved][cols])
+ *   seeds from std::srand/std::rand        src/umcx.cpp:724-727  (-> umcx_seeds_from_rngseed)
+ * Entry points with no reference counterpart (the reference has no adjoint, replay or batching) say so.
+ */
+#ifndef UMCX_GPU_H
+#define UMCX_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UMCX_ABI_VERSION 1
+
+/* status codes */
+enum {
+    UMCX_OK = 0,
+    UMCX_ERR_INPUT = 1,   /* invalid argument or configuration (reference: std::runtime_error, L514/L520/L570/L667) */
+    UMCX_ERR_CUDA = 2,    /* a CUDA runtime call failed */
+    UMCX_ERR_TIMEOUT = 3, /* the device-side step cap or deadline was hit; partial results are returned */
+    UMCX_ERR_NODEV = 4    /* no usable CUDA device */
+};
+
+/* output types, same order as the reference's "xfe" (L57-58) */
+enum { UMCX_OUT_FLUENCE_RATE = 0, UMCX_OUT_FLUENCE = 1, UMCX_OUT_ENERGY = 2 };
+/* source types, same order as the reference's list (L59-60) */
+enum { UMCX_SRC_PENCIL = 0, UMCX_SRC_ISOTROPIC = 1, UMCX_SRC_CONE = 2, UMCX_SRC_DISK = 3, UMCX_SRC_PLANAR = 4,
+       UMCX_SRC_FOURIER = 5 };
+/* detected-photon record flags (L65) */
+enum { UMCX_DET_ID = 1, UMCX_DET_PPATH = 4, UMCX_DET_EXITPOS = 16, UMCX_DET_EXITDIR = 32 };
+
+/* bit 7 of a label byte marks a detector voxel (the reference uses the sign bit of an int32 label, L35-36, L622) */
+#define UMCX_LABEL_DET 0x80u
+#define UMCX_LABEL_MASK 0x7Fu
+/* largest medium count: labels are 7-bit */
+#define UMCX_MAX_MEDIA 128
+/* largest detector count handled by the device kernels */
+#define UMCX_MAX_DET 64
+/* largest time-gate count */
+#define UMCX_MAX_GATES 65535
+
+/* umcx_sim.flags bits */
+#define UMCX_SIM_STRICT_MATH 0x1u /* evaluate every expression like the reference (IEEE division, expf/logf/
+                                     sinf/cosf/acosf, no FMA contraction) instead of the fast hardware forms */
+#define UMCX_SIM_FLAGS_ALL 0x1u
+
+/*
+ * One simulation.  Field meanings follow MCX_param (L95-99) as filled at L787-796, plus the inputs MCX_kernel
+ * reads itself (photon count L726, seeds L725-727, source L728-729).  mua and mus in the media table are in
+ * per-voxel units, i.e. already multiplied by unitinmm as at L804.
+ */
+typedef struct umcx_sim {
+    uint32_t dim[4];          /* nx, ny, nz, maxgate (L789) */
+    uint64_t nphoton;         /* photons to launch */
+    uint64_t photon_offset;   /* index of the first photon; photon i is reseeded from (seeds, i) (L761) */
+    float tstart, tend, rtstep, unitinmm;
+    int32_t isreflect;        /* DoMismatch */
+    int32_t issavevol;        /* DoSaveVolume */
+    int32_t issavedet;        /* DoPartialPath */
+    int32_t savedetflag;      /* SaveDetFlag, sum of UMCX_DET_* */
+    int32_t mediumnum;        /* media count including label 0 */
+    int32_t outputtype;       /* UMCX_OUT_* */
+    int32_t detnum;           /* detectors */
+    int32_t srctype;          /* UMCX_SRC_* */
+    uint32_t maxdetphotons;   /* MaxDetPhoton */
+    uint32_t flags;           /* UMCX_SIM_* bits (0 = production fast path) */
+    uint32_t seeds[4];        /* the four 32-bit session seeds */
+    float srcpos[4];          /* source position (w = initial weight, 1) */
+    float srcdir[4];          /* source direction */
+    float srcparam1[4];
+    float srcparam2[4];
+} umcx_sim;
+
+/* Per-call results (not normalised; the host applies the normaliser of L820). */
+typedef struct umcx_result {
+    double energy_escape;     /* L768-769 */
+    double energy_total;      /* L766-767 */
+    uint64_t detected;        /* MCX_detect::detectedphoton: all detections, including those beyond maxdetphotons */
+    uint64_t saved;           /* MCX_detect::savedcount() */
+    uint64_t launched;        /* photons processed */
+    uint64_t steps;           /* voxel steps (MCX_photon::step calls) */
+    uint64_t crossings;       /* voxel changes (deposit sites) */
+    uint64_t scatters;        /* scattering events */
+    uint64_t reflections;     /* MCX_photon::reflect calls */
+    uint64_t capped;          /* photons terminated by the per-photon step cap (0 in a normal run) */
+    float kernel_ms;          /* device time of the propagation kernel (CUDA events) */
+    float total_ms;           /* wall time of the whole call */
+    int32_t status;           /* same as the return value */
+    int32_t reserved;
+} umcx_result;
+
+/* Launch tuning; zero fields mean "choose automatically" (autotuner cache or built-in default). */
+typedef struct umcx_tuning {
+    int32_t block_size;       /* threads per CTA */
+    int32_t blocks_per_sm;    /* resident CTAs per SM for the persistent grid */
+    int32_t aggregation;      /* 0 auto, 1 plain atomics, 2 warp match-any aggregation of fluence adds */
+    int32_t reserved;
+} umcx_tuning;
+
+typedef struct umcx_context umcx_context;
+
+/* library ABI version (UMCX_ABI_VERSION) */
+int umcx_abi_version(void);
+
+/* Create a context bound to CUDA device `device` (0-based; the reference's DeviceID is 1-based, L739). */
+int umcx_create(umcx_context** ctx, int device);
+void umcx_destroy(umcx_context* ctx);
+/* Message of the last failure on ctx (empty string if none).  Valid until the next call on ctx. */
+const char* umcx_last_error(const umcx_context* ctx);
+/* Set the launch tuning used by later calls on ctx (NULL resets to automatic). */
+int umcx_set_tuning(umcx_context* ctx, const umcx_tuning* tuning);
+
+/* The four session seeds for RNGSeed (L724-727): srand(seed) then four rand() calls of the C library;
+ * rngseed <= 0 uses the current time like the reference. */
+int umcx_seeds_from_rngseed(int32_t rngseed, uint32_t seeds[4]);
+
+/* Number of float columns of one detected-photon record (L157). */
+int umcx_detp_columns(const umcx_sim* sim);
+
+/*
+ * Forward simulation with HOST buffers (replaces MCX_kernel, L722-781).
+ *   labels   uint8 [nx][ny][nz] (z fastest), bit 7 = detector voxel
+ *   media    float [mediumnum][4] = {mua, mus, g, n}, per-voxel units
+ *   detpos   float [detnum][4]    = {x, y, z, radius} in voxels (may be NULL when detnum == 0)
+ *   fluence  float [maxgate][nx][ny][nz], overwritten (may be NULL when issavevol == 0)
+ *   detp     float [maxdetphotons][umcx_detp_columns(sim)] (may be NULL when issavedet == 0)
+ * Copies in, runs the persistent propagation kernel, copies out, synchronises.
+ */
+int umcx_gpu_forward(umcx_context* ctx, const umcx_sim* sim, const uint8_t* labels, const float* media,
+                     const float* detpos, float* fluence, float* detp, umcx_result* res);
+
+/*
+ * Forward simulation with DEVICE buffers d_labels, d_fluence, d_detp (same layouts as above; media and
+ * detpos are host arrays) on `stream` (a cudaStream_t, NULL = legacy default stream).  Synchronises the
+ * stream before returning and fills res.
+ */
+int umcx_gpu_forward_device(umcx_context* ctx, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
+                            const float* detpos, float* d_fluence, float* d_detp, void* stream, umcx_result* res);
+
+/*
+ * Debug known-answer hook for the random number generator (MCX_rand, L187-215): for photons
+ * photon_offset .. photon_offset+nphoton-1 of sim, writes `ndraw` consecutive rand01() values of each photon
+ * to out[nphoton][ndraw] (host buffer), computed on the device.
+ */
+int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photon_offset, uint32_t nphoton,
+                      uint32_t ndraw, float* out);
+
+/* Command-line and JSON entry points of the reference (L850-856), running the simulation on the GPU and
+ * writing the same console line and output files.  They return 0 on success and non-zero on failure. */
+int MCX_run_cmd(char* argv[], int argn);
+int MCX_run_json(char* jsoninput);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UMCX_GPU_H */

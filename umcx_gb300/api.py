@@ -1,0 +1,227 @@
+"""Python side of the library: jobs (reference-style inputs) and GPU contexts, over the C ABI.
+
+    from umcx_gb300 import Job, Context
+    job = Job.from_args(["--bench", "cube60", "-n", "1e6"])
+    with Context(0) as ctx:
+        out = ctx.forward(job.sim, job.labels, job.media, job.detpos)
+    out.fluence  # float32 [maxgate, nx, ny, nz], not normalised; job.normalizer(out.energy_total) gives L820's factor
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import Result, Sim, Tuning, check, load
+
+
+def _argv(args: list[str]):
+    arr = (C.c_char_p * (len(args) + 1))()
+    arr[0] = b"umcx"
+    for k, a in enumerate(args):
+        arr[k + 1] = a.encode()
+    return arr
+
+
+class Job:
+    """A parsed reference-style input (MCX_userio + MCX_run_simulation set-up)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_args(cls, args: list[str]) -> "Job":
+        lib = load()
+        h = C.c_void_p()
+        rc = lib.umcx_job_from_args(C.byref(h), len(args) + 1, _argv(args))
+        job = cls(h)
+        if rc != _lib.UMCX_OK:
+            msg = lib.umcx_job_error(h).decode()
+            lib.umcx_job_free(h)
+            job._h = None
+            raise ValueError(msg)
+        return job
+
+    @classmethod
+    def from_json(cls, cfg) -> "Job":
+        text = cfg if isinstance(cfg, str) else json.dumps(cfg)
+        return cls.from_args(["--json", text])
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            load().umcx_job_free(self._h)
+            self._h = None
+
+    @property
+    def action(self) -> int:
+        return load().umcx_job_action(self._h)
+
+    @property
+    def console(self) -> str:
+        return load().umcx_job_console(self._h).decode()
+
+    @property
+    def config(self) -> dict:
+        return json.loads(load().umcx_job_config_json(self._h, -1).decode())
+
+    @property
+    def sim(self) -> Sim:
+        return load().umcx_job_sim(self._h).contents.copy()
+
+    @property
+    def labels(self) -> np.ndarray:
+        s = self.sim
+        n = s.dim[0] * s.dim[1] * s.dim[2]
+        p = load().umcx_job_labels(self._h)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy().reshape(s.dim[0], s.dim[1], s.dim[2])
+
+    @property
+    def media(self) -> np.ndarray:
+        s = self.sim
+        p = load().umcx_job_media(self._h)
+        return np.ctypeslib.as_array(p, shape=(s.mediumnum * 4,)).copy().reshape(s.mediumnum, 4)
+
+    @property
+    def detpos(self) -> np.ndarray:
+        s = self.sim
+        if s.detnum == 0:
+            return np.zeros((0, 4), np.float32)
+        p = load().umcx_job_detpos(self._h)
+        return np.ctypeslib.as_array(p, shape=(s.detnum * 4,)).copy().reshape(s.detnum, 4)
+
+    @property
+    def isnormalized(self) -> bool:
+        return bool(load().umcx_job_isnormalized(self._h))
+
+    def normalizer(self, energytotal: float) -> float:
+        return float(load().umcx_job_normalizer(self._h, energytotal))
+
+    def domain_int32(self) -> np.ndarray:
+        lib = load()
+        dims = (C.c_uint32 * 3)()
+        check(lib.umcx_job_domain_dims(self._h, dims), None, "umcx_job_domain_dims")
+        out = np.zeros(dims[0] * dims[1] * dims[2], np.int32)
+        check(lib.umcx_job_domain_int32(self._h, out.ctypes.data, out.size), None, "umcx_job_domain_int32")
+        return out.reshape(dims[0], dims[1], dims[2])
+
+    def dump_mask(self, path: str) -> None:
+        check(load().umcx_job_dump_mask(self._h, path.encode()), None, "umcx_job_dump_mask")
+
+    def write_outputs(self, fluence, detp, res: Result, normalize: bool = True) -> None:
+        f = None if fluence is None else np.ascontiguousarray(fluence, np.float32)
+        d = None if detp is None else np.ascontiguousarray(detp, np.float32)
+        check(load().umcx_job_write_outputs(self._h, None if f is None else f.ctypes.data,
+                                            None if d is None else d.ctypes.data, C.byref(res), int(normalize)),
+              None, "umcx_job_write_outputs")
+
+
+def detp_columns(sim: Sim) -> int:
+    return load().umcx_detp_columns(C.byref(sim))
+
+
+def seeds_from_rngseed(seed: int) -> np.ndarray:
+    out = (C.c_uint32 * 4)()
+    check(load().umcx_seeds_from_rngseed(int(seed), out), None, "umcx_seeds_from_rngseed")
+    return np.array(list(out), np.uint32)
+
+
+@dataclass
+class Forward:
+    fluence: np.ndarray | None
+    detp: np.ndarray | None
+    result: Result
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def energy_total(self) -> float:
+        return self.result.energy_total
+
+    @property
+    def energy_escape(self) -> float:
+        return self.result.energy_escape
+
+    @property
+    def absorbed_fraction(self) -> float:
+        r = self.result
+        return (r.energy_total - r.energy_escape) / r.energy_total
+
+
+class Context:
+    """A CUDA device context of the library (umcx_create / umcx_destroy)."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        self._h = C.c_void_p()
+        rc = lib.umcx_create(C.byref(self._h), int(device))
+        if rc != _lib.UMCX_OK:
+            raise RuntimeError(f"umcx_create({device}) failed with status {rc}")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().umcx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self) -> str:
+        return load().umcx_last_error(self._h).decode()
+
+    def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0) -> None:
+        t = Tuning(block_size, blocks_per_sm, aggregation, 0)
+        check(load().umcx_set_tuning(self._h, C.byref(t)), self._h, "umcx_set_tuning")
+
+    def forward(self, sim: Sim, labels, media, detpos=None) -> Forward:
+        """Host-buffer forward simulation (umcx_gpu_forward)."""
+        lab = np.ascontiguousarray(labels, np.uint8)
+        med = np.ascontiguousarray(media, np.float32)
+        det = np.ascontiguousarray(detpos if detpos is not None else np.zeros((0, 4)), np.float32)
+        nout = sim.dim[0] * sim.dim[1] * sim.dim[2] * sim.dim[3]
+        flu = np.zeros(nout, np.float32) if sim.issavevol else None
+        cols = detp_columns(sim)
+        dp = np.zeros(max(1, sim.maxdetphotons * cols), np.float32) if sim.issavedet else None
+        res = Result()
+        rc = load().umcx_gpu_forward(self._h, C.byref(sim), lab.ctypes.data, med.ctypes.data,
+                                     det.ctypes.data if det.size else None,
+                                     None if flu is None else flu.ctypes.data,
+                                     None if dp is None else dp.ctypes.data, C.byref(res))
+        check(rc, self._h, "umcx_gpu_forward")
+        if flu is not None:
+            flu = flu.reshape(sim.dim[3], sim.dim[0], sim.dim[1], sim.dim[2])
+        if dp is not None:
+            dp = dp[: res.saved * cols].reshape(res.saved, cols)
+        return Forward(flu, dp, res)
+
+    def forward_device(self, sim: Sim, d_labels, media, detpos, d_fluence, d_detp, stream=None) -> Result:
+        """Device-buffer forward simulation (umcx_gpu_forward_device); d_* are torch CUDA tensors."""
+        med = np.ascontiguousarray(media, np.float32)
+        det = np.ascontiguousarray(detpos if detpos is not None else np.zeros((0, 4)), np.float32)
+        res = Result()
+        st = None if stream is None else C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+        rc = load().umcx_gpu_forward_device(self._h, C.byref(sim), C.c_void_p(d_labels.data_ptr()), med.ctypes.data,
+                                            det.ctypes.data if det.size else None,
+                                            None if d_fluence is None else C.c_void_p(d_fluence.data_ptr()),
+                                            None if d_detp is None else C.c_void_p(d_detp.data_ptr()), st,
+                                            C.byref(res))
+        check(rc, self._h, "umcx_gpu_forward_device")
+        return res
+
+    def rng_dump(self, seeds, photon_offset: int, nphoton: int, ndraw: int) -> np.ndarray:
+        s = (C.c_uint32 * 4)(*[int(x) for x in seeds])
+        out = np.zeros(nphoton * ndraw, np.float32)
+        check(load().umcx_gpu_rng_dump(self._h, s, int(photon_offset), int(nphoton), int(ndraw), out.ctypes.data),
+              self._h, "umcx_gpu_rng_dump")
+        return out.reshape(nphoton, ndraw)

@@ -1,0 +1,106 @@
+// kernels_fast.cu - instances of the production (fast-math) propagation kernels, the launch policy and the RNG
+// known-answer kernel.
+#include <algorithm>
+
+#include "launch.h"
+
+namespace umcx_dev {
+
+template <bool R, bool D>
+static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
+    k_forward<false, R, D><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+}
+
+void launch_forward_fast(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
+    if (lc.reflect) {
+        if (lc.savedet) launch_one<true, true>(lc, P, B, st);
+        else launch_one<true, false>(lc, P, B, st);
+    } else {
+        if (lc.savedet) launch_one<false, true>(lc, P, B, st);
+        else launch_one<false, false>(lc, P, B, st);
+    }
+}
+
+template <bool R, bool D>
+static int occ_one(int block, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_forward<false, R, D>, block, smem) != cudaSuccess) return 0;
+    return n;
+}
+
+// allow the forward kernels up to 227 KB of dynamic shared memory (large per-thread partial-path scratch)
+template <bool R, bool D>
+static cudaError_t allow_big_smem() {
+    return cudaFuncSetAttribute(k_forward<false, R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+cudaError_t configure_fast_kernels() {
+    cudaError_t e = allow_big_smem<false, false>();
+    if (e == cudaSuccess) e = allow_big_smem<false, true>();
+    if (e == cudaSuccess) e = allow_big_smem<true, false>();
+    if (e == cudaSuccess) e = allow_big_smem<true, true>();
+    return e;
+}
+
+int occupancy_fast(bool reflect, bool savedet, int block, size_t smem) {
+    if (reflect) return savedet ? occ_one<true, true>(block, smem) : occ_one<true, false>(block, smem);
+    return savedet ? occ_one<false, true>(block, smem) : occ_one<false, false>(block, smem);
+}
+
+void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st, bool strict) {
+    if (strict) launch_forward_strict(lc, P, B, st);
+    else launch_forward_fast(lc, P, B, st);
+}
+
+size_t forward_smem(const KParams& P, int block, bool savedet) {
+    size_t s = sizeof(Medium) * static_cast<size_t>(P.mediumnum);
+    if (savedet) s += sizeof(float) * static_cast<size_t>(P.ppathlen) * static_cast<size_t>(block);
+    s += sizeof(float) * static_cast<size_t>(block);  // aggregation buffer
+    return s;
+}
+
+int forward_occupancy(bool strict, bool reflect, bool savedet, int block, size_t smem) {
+    return strict ? occupancy_strict(reflect, savedet, block, smem) : occupancy_fast(reflect, savedet, block, smem);
+}
+
+LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const umcx_sim* s, const KParams& P) {
+    (void)device;
+    LaunchChoice lc;
+    lc.reflect = s->isreflect != 0;
+    lc.savedet = s->issavedet != 0;
+    const bool strict = (s->flags & UMCX_SIM_STRICT_MATH) != 0;
+    lc.block = t.block_size > 0 ? t.block_size : 256;
+    lc.aggregate = t.aggregation == 2 ? 1 : 0;
+    lc.smem = forward_smem(P, lc.block, lc.savedet);
+    int occ = forward_occupancy(strict, lc.reflect, lc.savedet, lc.block, lc.smem);
+    if (occ < 1) occ = 1;
+    const int per_sm = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
+    lc.grid = sm_count * per_sm;
+    // never launch more lanes than photons need (small runs): whole warps, at least one CTA
+    const unsigned long long lanes = static_cast<unsigned long long>(lc.grid) * lc.block;
+    if (P.nphoton < lanes) {
+        unsigned long long g = (P.nphoton + lc.block - 1) / lc.block;
+        lc.grid = static_cast<int>(std::max<unsigned long long>(1ULL, g));
+    }
+    return lc;
+}
+
+__global__ void k_rng_dump(unsigned s0, unsigned s1, unsigned s2, unsigned s3, unsigned long long offset,
+                           unsigned nphoton, unsigned ndraw, float* out) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nphoton) return;
+    const unsigned long long idx = offset + i;
+    const unsigned i32 = static_cast<unsigned>(idx);
+    Rng r;
+    rng_reseed(r, s0 ^ i32, s1 | i32, s2 ^ i32, s3 | i32);
+    float* o = out + static_cast<unsigned long long>(i) * ndraw;
+    for (unsigned k = 0; k < ndraw; k++) o[k] = rng_rand01(r);
+}
+
+void launch_rng_dump(const uint32_t seeds[4], unsigned long long offset, unsigned nphoton, unsigned ndraw, float* out,
+                     cudaStream_t stream) {
+    const unsigned block = 128;
+    const unsigned grid = (nphoton + block - 1) / block;
+    if (grid) k_rng_dump<<<grid, block, 0, stream>>>(seeds[0], seeds[1], seeds[2], seeds[3], offset, nphoton, ndraw, out);
+}
+
+}  // namespace umcx_dev

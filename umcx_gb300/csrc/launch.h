@@ -1,0 +1,40 @@
+// launch.h - launch configuration and the per-translation-unit kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/umcx_gpu.h"
+#include "propagate.cuh"
+
+namespace umcx_dev {
+
+struct LaunchChoice {
+    int block = 256;
+    int grid = 0;
+    int aggregate = 0;
+    size_t smem = 0;
+    bool reflect = false;
+    bool savedet = false;
+};
+
+// dynamic shared memory of the forward kernel for a block size
+size_t forward_smem(const KParams& P, int block, bool savedet);
+
+// resident CTAs per SM of a forward kernel instance (0 on error)
+int forward_occupancy(bool strict, bool reflect, bool savedet, int block, size_t smem);
+
+// grid = SM count x resident CTAs (persistent kernel), block size and aggregation from the tuning or defaults
+LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const umcx_sim* s, const KParams& P);
+
+void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream, bool strict);
+void launch_forward_fast(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream);
+void launch_forward_strict(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream);
+int occupancy_fast(bool reflect, bool savedet, int block, size_t smem);
+cudaError_t configure_fast_kernels();
+cudaError_t configure_strict_kernels();
+int occupancy_strict(bool reflect, bool savedet, int block, size_t smem);
+
+void launch_rng_dump(const uint32_t seeds[4], unsigned long long offset, unsigned nphoton, unsigned ndraw, float* out,
+                     cudaStream_t stream);
+
+}  // namespace umcx_dev
