@@ -1,0 +1,346 @@
+"""Benchmark of the umcx photon-transport hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--photons P]
+
+Workload: the heterogeneous forward configuration with refractive mismatch and detectors -- 60x60x60 voxels of
+1 mm, background label 1 (mua 0.005/mm, mus 1/mm, g 0.01, n 1.37), a radius-15 sphere of label 2 (mua 0.002,
+mus 5, g 0.9, n 1.0) centred at (30,30,30), pencil source at (29,29,0) along +z, boundary reflection on, 1e7
+photons per step, 50 time gates over 0-5 ns, four disk detectors of radius 1 mm at z = 0 with partial
+pathlengths saved.  Synthetic input (the configuration is generated, not read from a dataset).
+
+One step = one full simulation of P photons.  `value` is photons/ms of the propagation kernel with the inputs
+resident in HBM (CUDA events on the launching stream; the fluence output, 43 MB, is cleared inside the step and the
+L2 is flushed by writing a 256 MB buffer between steps).  `e2e` is the same metric through the C ABI call with host
+buffers (umcx_gpu_forward: label upload, simulation, fluence + detected-photon download), timed on the host.
+
+--impl reference times the reference's own CPU implementation (the unmodified reference program built from its
+sources, oracle/_ref/umcx, with all host threads; else the C restatement in oracle/) on a bounded photon sample of
+the same configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIG = {
+    "Session": {"ID": "bench_c2", "Photons": 10000000, "RNGSeed": 1648335518, "DoMismatch": 1, "DoPartialPath": 1,
+                "SaveDetFlag": 5, "OutputType": "x"},
+    "Forward": {"T0": 0, "T1": 5e-9, "Dt": 1e-10},
+    "Domain": {"Dim": [60, 60, 60], "LengthUnit": 1,
+               "Media": [{"mua": 0, "mus": 0, "g": 1, "n": 1}, {"mua": 0.005, "mus": 1.0, "g": 0.01, "n": 1.37},
+                         {"mua": 0.002, "mus": 5.0, "g": 0.9, "n": 1.0}]},
+    "Optode": {"Source": {"Type": "pencil", "Pos": [29, 29, 0], "Dir": [0, 0, 1]},
+               "Detector": [{"Pos": [29, 19, 0], "R": 1}, {"Pos": [19, 29, 0], "R": 1},
+                            {"Pos": [29, 39, 0], "R": 1}, {"Pos": [39, 29, 0], "R": 1}]},
+    "Shapes": [{"Grid": {"Tag": 1, "Size": [60, 60, 60]}}, {"Sphere": {"O": [30, 30, 30], "R": 15, "Tag": 2}}],
+}
+WORKLOAD = "heterogeneous forward, 60^3 grid, sphere R15, reflection on, 50 gates, 4 detectors (ppath saved)"
+METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates, 4 detectors)"
+
+# per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
+# step L316-337, scatter L364-380, voxel crossing / deposit L285-310, reflect L381-417
+OPS_FP32 = {"steps": 26, "scatters": 45, "crossings": 8, "reflections": 25}
+OPS_SFU = {"steps": 2, "scatters": 9, "crossings": 1, "reflections": 2}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_run(photons: int, threads: int) -> dict:
+    """Run the reference's CPU implementation on the benchmark configuration; returns photons/ms and details."""
+    import oracle
+
+    cfg = json.loads(json.dumps(CONFIG))
+    cfg["Session"]["Photons"] = int(photons)
+    cfg["Session"]["DoSaveVolume"] = 1
+    if oracle.have_reference():
+        with tempfile.TemporaryDirectory() as d:
+            t0 = time.perf_counter()
+            r = oracle.run_reference(["-j", json.dumps(cfg)], d, threads=threads, timeout=900)
+            wall = time.perf_counter() - t0
+        if r.get("returncode") == 0 and "speed" in r:
+            return {"value": r["speed"], "kind": "reference", "wall_s": wall, "duration_ms": r["duration_ms"],
+                    "absorbed": r["absorbed"], "detected": r["detected"]}
+    from umcx_gb300 import Job
+
+    job = Job.from_json(cfg)
+    t0 = time.perf_counter()
+    _, _, res, _ = oracle.forward(job.sim, job.labels, job.media, job.detpos, nthreads=threads)
+    ms = (time.perf_counter() - t0) * 1e3
+    return {"value": photons / ms, "kind": "port", "wall_s": ms / 1e3, "duration_ms": ms,
+            "absorbed": (res.energy_total - res.energy_escape) / res.energy_total * 100, "detected": int(res.saved)}
+
+
+def run_reference_arm(args) -> None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+
+    try:
+        oracle.build(reference_root="/root/reference" if Path("/root/reference").exists() else None)
+    except Exception:
+        pass
+    threads = os.cpu_count() or 1
+    photons = args.cpu_photons
+    for _ in range(args.warmup):
+        cpu_reference_run(max(photons // 10, 10000), threads)
+    vals, walls, info = [], [], None
+    for _ in range(args.steps):
+        info = cpu_reference_run(photons, threads)
+        vals.append(info["value"])
+        walls.append(info["wall_s"])
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "photons/ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (generated configuration)",
+        "config": {"workload": WORKLOAD, "photons_per_step": photons, "threads": threads,
+                   "program": "reference umcx CPU OpenMP build" if info["kind"] == "reference" else "oracle C port"},
+        "cpu_baseline": {"value": value, "unit": "photons/ms", "cores": threads, "kind": info["kind"],
+                         "sample": f"{photons} photons of the benchmark configuration per step"},
+        "e2e": {"value": value, "unit": "photons/ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+        "absorbed_percent": info["absorbed"], "detected": info["detected"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu_arm(args) -> None:
+    import numpy as np
+    import torch
+
+    from umcx_gb300 import Context, Job, measure_peaks
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if ws > 1 else 0
+    torch.cuda.set_device(device)
+
+    cfg = json.loads(json.dumps(CONFIG))
+    cfg["Session"]["Photons"] = int(args.photons)
+    job = Job.from_json(cfg)
+    sim = job.sim
+    sim.photon_offset = rank * int(args.photons)  # weak scaling: each rank simulates its own photon range
+    ctx = Context(device)
+    if args.block or args.blocks_per_sm or args.aggregation:
+        ctx.set_tuning(args.block, args.blocks_per_sm, args.aggregation)
+    nvox = sim.dim[0] * sim.dim[1] * sim.dim[2]
+    nout = nvox * sim.dim[3]
+    d_lab = torch.from_numpy(job.labels.ravel().copy()).to(f"cuda:{device}")
+    d_flu = torch.empty(nout, dtype=torch.float32, device=f"cuda:{device}")
+    d_det = torch.empty(sim.maxdetphotons * 4, dtype=torch.float32, device=f"cuda:{device}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        ctx.forward_device(sim, d_lab, job.media, job.detpos, d_flu, d_det, stream)
+    sampler = ClockSampler(device)
+    sampler.start()
+    kernel_ms, step_ms, results = [], [], []
+    barrier()
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        r = ctx.forward_device(sim, d_lab, job.media, job.detpos, d_flu, d_det, stream)
+        ev1.record(stream)
+        ev1.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+        kernel_ms.append(r.kernel_ms)
+        results.append(r)
+    barrier()
+    wall_all = time.perf_counter() - t_all
+    clocks = sampler.stop()
+
+    # end to end through the C ABI with host buffers
+    e2e_ms = []
+    for _ in range(max(1, args.e2e_steps)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = ctx.forward(sim, job.labels, job.media, job.detpos)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    r_host = out.result
+    h2d = nvox + 4 * 4 * sim.mediumnum + 4 * 4 * sim.detnum
+    d2h = nout * 4 + int(r_host.saved) * 4 * 4 + 96
+
+    # max over ranks
+    total_step_ms = sum(step_ms)
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_step_ms, statistics.mean(e2e_ms)], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_step_ms, e2e_mean = t.tolist()
+    else:
+        e2e_mean = statistics.mean(e2e_ms)
+
+    photons_all = int(args.photons) * ws
+    value = photons_all * args.steps / total_step_ms
+    e2e_value = photons_all / e2e_mean
+    r0 = results[-1]
+    kms = statistics.mean(kernel_ms)
+    fp32_ops = sum(getattr(r0, k) * v for k, v in OPS_FP32.items())
+    sfu_ops = sum(getattr(r0, k) * v for k, v in OPS_SFU.items())
+    peaks = measure_peaks(device)
+    achieved_fp32 = fp32_ops / (kms * 1e-3) / 1e12
+    peak_fp32 = peaks["fp32_fma_per_s"] / 1e12
+    achieved_sfu = sfu_ops / (kms * 1e-3) / 1e12
+    peak_sfu = peaks["sfu_per_s"] / 1e12
+    atomics_per_s = r0.crossings / (kms * 1e-3)
+    peaks_file = ROOT / "MEASURED_PEAKS.json"
+    hbm_peak = json.loads(peaks_file.read_text()).get("hbm_gbs") if peaks_file.exists() else 6800.0
+    traffic_alg = r0.crossings * 9.0  # label byte + fluence read-modify-write per crossing
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_reference_run(args.cpu_photons, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "photons/ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_step_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (generated configuration)",
+            "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": int(args.photons), "grid": [60, 60, 60],
+                       "gates": int(sim.dim[3]), "detectors": int(sim.detnum),
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"photon ranges x{ws}"},
+            "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},
+            "gpu_launches": args.steps,
+            "kernel_ms": kms,
+            "roofline": {"bound": "fp32", "achieved": achieved_fp32, "peak": peak_fp32,
+                         "unit": "Top/s (FP32 instructions, FMA = 1 op; peak measured live by an FMA loop)",
+                         "frac": achieved_fp32 / peak_fp32, "traffic": None,
+                         "ops_per_launch": fp32_ops,
+                         "events_per_launch": {k: int(getattr(r0, k)) for k in OPS_FP32},
+                         "sfu": {"achieved": achieved_sfu, "peak": peak_sfu, "frac": achieved_sfu / peak_sfu,
+                                 "unit": "Top/s"},
+                         "l2_atomics": {"achieved_per_s": atomics_per_s, "peak_per_s": peaks["l2_atomic_per_s"],
+                                        "frac": atomics_per_s / peaks["l2_atomic_per_s"]},
+                         "hbm": {"algorithmic_gbs": traffic_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak}},
+            "clocks": clocks,
+            "physics": {"absorbed_percent": (r0.energy_total - r0.energy_escape) / r0.energy_total * 100,
+                        "detected": int(r0.detected), "steps_per_photon": r0.steps / r0.launched,
+                        "scatters_per_photon": r0.scatters / r0.launched},
+            "wall_s_timed": wall_all,
+        }
+        if cpu:
+            line["cpu_baseline"] = {"value": cpu["value"], "unit": "photons/ms", "cores": os.cpu_count() or 1,
+                                    "kind": cpu["kind"],
+                                    "sample": f"{args.cpu_photons} photons of the same configuration"}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--photons", type=float, default=1e7)
+    ap.add_argument("--cpu-photons", type=int, default=1000000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--aggregation", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        if args.cpu_photons == 1000000:
+            args.cpu_photons = 300000
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

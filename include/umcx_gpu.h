@@ -58,7 +58,11 @@ enum { UMCX_DET_ID = 1, UMCX_DET_PPATH = 4, UMCX_DET_EXITPOS = 16, UMCX_DET_EXIT
 /* umcx_sim.flags bits */
 #define UMCX_SIM_STRICT_MATH 0x1u /* evaluate every expression like the reference (IEEE division, expf/logf/
                                      sinf/cosf/acosf, no FMA contraction) instead of the fast hardware forms */
-#define UMCX_SIM_FLAGS_ALL 0x1u
+#define UMCX_SIM_FP32_ACCUM 0x2u /* accumulate the output volume with FP32 atomics directly in `fluence`, like the
+                                    reference (MCX_volume::add, L134-137).  Default: FP64 accumulation in a
+                                    library-owned volume, rounded to FP32 once at the end; FP32 accumulation loses
+                                    small deposits in heavily hit voxels (2e-5 of the energy at 1e6 photons). */
+#define UMCX_SIM_FLAGS_ALL 0x3u
 
 /*
  * One simulation.  Field meanings follow MCX_param (L95-99) as filled at L787-796, plus the inputs MCX_kernel
@@ -110,7 +114,8 @@ typedef struct umcx_tuning {
     int32_t block_size;       /* threads per CTA */
     int32_t blocks_per_sm;    /* resident CTAs per SM for the persistent grid */
     int32_t aggregation;      /* 0 auto, 1 plain atomics, 2 warp match-any aggregation of fluence adds */
-    int32_t reserved;
+    int32_t budget_ms;        /* wall-clock budget of one propagation launch; 0 = 600 000 ms.  When it runs out the
+                                 kernel stops, the call returns UMCX_ERR_TIMEOUT and the context stays usable. */
 } umcx_tuning;
 
 typedef struct umcx_context umcx_context;
@@ -160,6 +165,17 @@ int umcx_gpu_forward_device(umcx_context* ctx, const umcx_sim* sim, const uint8_
  */
 int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photon_offset, uint32_t nphoton,
                       uint32_t ndraw, float* out);
+
+/* Roofline denominators measured on the device (no reference counterpart): FP32 FMA instructions per second,
+ * SFU (MUFU) operations per second and scattered float atomicAdd operations per second into an L2-resident array. */
+typedef struct umcx_peaks {
+    double fp32_fma_per_s;
+    double sfu_per_s;
+    double l2_atomic_per_s;
+    int32_t sm_count;
+    int32_t sm_clock_khz;
+} umcx_peaks;
+int umcx_measure_peaks(int device, umcx_peaks* out);
 
 /* Command-line and JSON entry points of the reference (L850-856), running the simulation on the GPU and
  * writing the same console line and output files.  They return 0 on success and non-zero on failure. */

@@ -14,9 +14,9 @@ REF=${1:-/root/reference}
 OUT="$HERE/_ref"
 mkdir -p "$OUT/src/nlohmann" "$OUT/src/zmat"
 if [ -f "$REF/src/umcx.cpp" ]; then
-    cp "$REF/src/umcx.cpp" "$OUT/src/umcx.cpp"
-    cp "$REF/src/nlohmann/json.hpp" "$OUT/src/nlohmann/json.hpp"
-    cp "$REF/src/zmat/zmat.h" "$OUT/src/zmat/zmat.h"
+    cp -p "$REF/src/umcx.cpp" "$OUT/src/umcx.cpp"
+    cp -p "$REF/src/nlohmann/json.hpp" "$OUT/src/nlohmann/json.hpp"
+    cp -p "$REF/src/zmat/zmat.h" "$OUT/src/zmat/zmat.h"
 fi
 if [ ! -f "$OUT/src/umcx.cpp" ]; then
     echo "build_ref: reference sources not found (neither $REF/src nor $OUT/src)" >&2

@@ -16,6 +16,7 @@ SRC_TYPES = ["pencil", "isotropic", "cone", "disk", "planar", "fourier"]
 DET_ID, DET_PPATH, DET_EXITPOS, DET_EXITDIR = 1, 4, 16, 32
 LABEL_DET = 0x80
 SIM_STRICT_MATH = 0x1
+SIM_FP32_ACCUM = 0x2
 ACTION_RUN, ACTION_DUMPJSON, ACTION_DUMPMASK, ACTION_HELP = 0, 1, 2, 3
 
 
@@ -77,7 +78,12 @@ class Result(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("aggregation", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("budget_ms", C.c_int32)]
+
+
+class Peaks(C.Structure):
+    _fields_ = [("fp32_fma_per_s", C.c_double), ("sfu_per_s", C.c_double), ("l2_atomic_per_s", C.c_double),
+                ("sm_count", C.c_int32), ("sm_clock_khz", C.c_int32)]
 
 
 assert C.sizeof(Sim) == 168, C.sizeof(Sim)
@@ -98,6 +104,7 @@ SIGNATURES = [
     ("umcx_gpu_forward", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, C.POINTER(Result)]),
     ("umcx_gpu_forward_device", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, _P, C.POINTER(Result)]),
     ("umcx_gpu_rng_dump", C.c_int, [_P, C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32, C.c_uint32, _P]),
+    ("umcx_measure_peaks", C.c_int, [C.c_int, C.POINTER(Peaks)]),
     ("MCX_run_cmd", C.c_int, [C.POINTER(C.c_char_p), C.c_int]),
     ("MCX_run_json", C.c_int, [C.c_char_p]),
     ("umcx_main", C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),

@@ -122,6 +122,14 @@ def detp_columns(sim: Sim) -> int:
     return load().umcx_detp_columns(C.byref(sim))
 
 
+def measure_peaks(device: int = 0) -> dict:
+    """FP32 FMA/s, SFU op/s and scattered L2 float-atomic/s of the device (roofline denominators)."""
+    p = _lib.Peaks()
+    check(load().umcx_measure_peaks(int(device), C.byref(p)), None, "umcx_measure_peaks")
+    return {"fp32_fma_per_s": p.fp32_fma_per_s, "sfu_per_s": p.sfu_per_s, "l2_atomic_per_s": p.l2_atomic_per_s,
+            "sm_count": p.sm_count, "sm_clock_khz": p.sm_clock_khz}
+
+
 def seeds_from_rngseed(seed: int) -> np.ndarray:
     out = (C.c_uint32 * 4)()
     check(load().umcx_seeds_from_rngseed(int(seed), out), None, "umcx_seeds_from_rngseed")
@@ -180,8 +188,9 @@ class Context:
     def last_error(self) -> str:
         return load().umcx_last_error(self._h).decode()
 
-    def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0) -> None:
-        t = Tuning(block_size, blocks_per_sm, aggregation, 0)
+    def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0,
+                   budget_ms: int = 0) -> None:
+        t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms)
         check(load().umcx_set_tuning(self._h, C.byref(t)), self._h, "umcx_set_tuning")
 
     def forward(self, sim: Sim, labels, media, detpos=None) -> Forward:

@@ -30,6 +30,7 @@ CU_UNITS = {
     "capi.cu": [],
     "kernels_fast.cu": [],
     "kernels_strict.cu": ["--fmad=false"],
+    "peaks.cu": [],
 }
 CPP_UNITS = ["jsonlite.cpp", "frontend.cpp", "run.cpp"]
 

@@ -48,7 +48,7 @@ struct umcx_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
     umcx_tuning tuning{};
-    DevBuf labels, fluence, detp, media, stats, counter, scratch;
+    DevBuf labels, fluence, detp, media, stats, counter, scratch, accum64;
 };
 
 namespace {
@@ -61,6 +61,11 @@ struct CudaError : std::exception {
 struct InputError : std::exception {
     std::string msg;
     explicit InputError(std::string m) : msg(std::move(m)) {}
+    const char* what() const noexcept override { return msg.c_str(); }
+};
+struct BudgetError : std::exception {
+    std::string msg;
+    explicit BudgetError(std::string m) : msg(std::move(m)) {}
     const char* what() const noexcept override { return msg.c_str(); }
 };
 
@@ -81,6 +86,9 @@ int guarded(umcx_context* ctx, F&& f) {
     } catch (const CudaError& e) {
         if (ctx) ctx->err = e.what();
         return UMCX_ERR_CUDA;
+    } catch (const BudgetError& e) {
+        if (ctx) ctx->err = e.what();
+        return UMCX_ERR_TIMEOUT;
     } catch (const std::bad_alloc&) {
         if (ctx) ctx->err = "host memory allocation failed";
         return UMCX_ERR_INPUT;
@@ -179,7 +187,13 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     UMCX_CK(cudaMemsetAsync(ctx->stats.ptr, 0, sizeof(KStats), stream));
     UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), stream));
     const size_t nout = 1ULL * s->dim[0] * s->dim[1] * s->dim[2] * s->dim[3];
-    if (s->issavevol) UMCX_CK(cudaMemsetAsync(d_fluence, 0, nout * sizeof(float), stream));
+    const bool fp64 = s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM);
+    if (fp64) {
+        UMCX_CK(ctx->accum64.ensure(nout * sizeof(double)));
+        UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, nout * sizeof(double), stream));
+    } else if (s->issavevol) {
+        UMCX_CK(cudaMemsetAsync(d_fluence, 0, nout * sizeof(float), stream));
+    }
 
     KBuffers B;
     std::memset(&B, 0, sizeof(B));
@@ -189,13 +203,19 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     B.media = static_cast<const Medium*>(ctx->media.ptr);
     B.stats = static_cast<KStats*>(ctx->stats.ptr);
     B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
+    B.fluence64 = fp64 ? static_cast<double*>(ctx->accum64.ptr) : nullptr;
 
     LaunchChoice lc = choose_launch(ctx->device, ctx->sm_count, ctx->tuning, s, P);
     P.aggregate = lc.aggregate;
+    if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
     UMCX_CK(cudaEventRecord(ctx->ev0, stream));
     launch_forward(lc, P, B, stream, (s->flags & UMCX_SIM_STRICT_MATH) != 0);
     UMCX_CK(cudaGetLastError());
     UMCX_CK(cudaEventRecord(ctx->ev1, stream));
+    if (fp64) {  // round the FP64 accumulation to the FP32 output once
+        launch_fp64_to_fp32(static_cast<const double*>(ctx->accum64.ptr), d_fluence, nout, ctx->sm_count, stream);
+        UMCX_CK(cudaGetLastError());
+    }
 }
 
 void collect(umcx_context* ctx, const umcx_sim* s, cudaStream_t stream, umcx_result* res) {
@@ -219,7 +239,7 @@ void collect(umcx_context* ctx, const umcx_sim* s, cudaStream_t stream, umcx_res
         res->kernel_ms = ms;
         res->status = st.error ? UMCX_ERR_TIMEOUT : UMCX_OK;
     }
-    if (st.error) throw CudaError("propagation kernel stopped at its wall-clock budget; results are partial");
+    if (st.error) throw BudgetError("propagation kernel stopped at its wall-clock budget; results are partial");
 }
 
 }  // namespace
@@ -266,6 +286,7 @@ void umcx_destroy(umcx_context* ctx) {
     ctx->stats.release();
     ctx->counter.release();
     ctx->scratch.release();
+    ctx->accum64.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -285,6 +306,7 @@ int umcx_set_tuning(umcx_context* ctx, const umcx_tuning* t) {
             throw InputError("block_size must be a multiple of 32 in 0..1024");
         if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) throw InputError("blocks_per_sm must be in 0..32");
         if (t->aggregation < 0 || t->aggregation > 2) throw InputError("aggregation must be 0, 1 or 2");
+        if (t->budget_ms < 0) throw InputError("budget_ms must be >= 0");
         ctx->tuning = *t;
         return UMCX_OK;
     });

@@ -84,6 +84,19 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     return lc;
 }
 
+__global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n) {
+    const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+        dst[i] = static_cast<float>(src[i]);
+}
+
+void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream) {
+    if (n == 0) return;
+    const unsigned long long blocks = (n + 255) / 256;
+    const int grid = static_cast<int>(blocks < static_cast<unsigned long long>(sm_count) * 8 ? blocks : sm_count * 8ULL);
+    k_fp64_to_fp32<<<grid, 256, 0, stream>>>(src, dst, n);
+}
+
 __global__ void k_rng_dump(unsigned s0, unsigned s1, unsigned s2, unsigned s3, unsigned long long offset,
                            unsigned nphoton, unsigned ndraw, float* out) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -34,6 +34,8 @@ cudaError_t configure_fast_kernels();
 cudaError_t configure_strict_kernels();
 int occupancy_strict(bool reflect, bool savedet, int block, size_t smem);
 
+void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream);
+
 void launch_rng_dump(const uint32_t seeds[4], unsigned long long offset, unsigned nphoton, unsigned ndraw, float* out,
                      cudaStream_t stream);
 

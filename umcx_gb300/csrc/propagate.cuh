@@ -90,6 +90,7 @@ struct KParams {
 struct KBuffers {
     const uint8_t* labels;
     float* fluence;
+    double* fluence64;   // optional FP64 accumulation volume (same layout as fluence)
     float* detp;
     const Medium* media;
     KStats* stats;
@@ -457,6 +458,15 @@ __device__ __forceinline__ float deposit_value(const KParams& P, const Photon& p
     else return (p.lw - p.pw) * m.b.y;
 }
 
+// one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
+// afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
+__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v) {
+    if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
+    else atomicAdd(B.fluence + idx, v);
+}
+
+__global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n);
+
 // =============================================================================================== the kernel
 // Shared memory layout: Medium[mediumnum] | float ppath[ppathlen][blockDim] | float aggbuf[blockDim] (aggregation)
 template <bool STRICT, bool REFLECT, bool SAVEDET>
@@ -590,15 +600,15 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
                         float s = 0.f;
                         const unsigned base = tid & ~31u;
                         for (unsigned g = grp; g; g &= g - 1) s += aggbuf[base + __ffs(g) - 1];
-                        atomicAdd(B.fluence + dep_idx, s);
+                        deposit_add(B, dep_idx, s);
                     }
                 }
                 __syncwarp();
             } else if (dep_idx >= 0) {
-                atomicAdd(B.fluence + dep_idx, dep_val);
+                deposit_add(B, dep_idx, dep_val);
             }
         } else if (dep_idx >= 0) {
-            atomicAdd(B.fluence + dep_idx, dep_val);
+            deposit_add(B, dep_idx, dep_val);
         }
 
         // ---- termination: energy tallies (L765-770) and detection (L276-278, L429-435)
