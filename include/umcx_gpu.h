@@ -166,6 +166,25 @@ int umcx_gpu_forward_device(umcx_context* ctx, const umcx_sim* sim, const uint8_
 int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photon_offset, uint32_t nphoton,
                       uint32_t ndraw, float* out);
 
+/*
+ * Allocation-free forward simulation.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc (an application that owns the device memory pool and forbids foreign
+ * allocations, a plugin living inside another framework's allocator, a real-time loop that must not allocate):
+ * same inputs and outputs as umcx_gpu_forward_device (device buffers d_labels, d_fluence, d_detp; host arrays
+ * media, detpos; a cudaStream_t), but no context, no allocation and no CUDA events.  The kernel's working state
+ * (photon counter, tallies, optical table) lives in one fixed device array of UMCX_NOALLOC_SCRATCH_BYTES inside the
+ * library, held by every GPU that loads it until the process exits; at most UMCX_NOALLOC_MAX_MEDIA media fit, and
+ * larger tables are rejected with UMCX_ERR_INPUT.  The output volume is accumulated in FP32 directly in d_fluence
+ * (as with UMCX_SIM_FP32_ACCUM).  The first call on a device looks up that array's address; make it before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps race and must be serialised by the
+ * caller.  res->kernel_ms is 0 (no events).
+ */
+#define UMCX_NOALLOC_SCRATCH_BYTES 8192
+#define UMCX_NOALLOC_MAX_MEDIA 128
+int umcx_gpu_forward_noalloc(int device, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
+                             const float* detpos, float* d_fluence, float* d_detp, void* stream, umcx_result* res);
+
 /* Roofline denominators measured on the device (no reference counterpart): FP32 FMA instructions per second,
  * SFU (MUFU) operations per second and scattered float atomicAdd operations per second into an L2-resident array. */
 typedef struct umcx_peaks {

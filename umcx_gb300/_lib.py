@@ -105,6 +105,7 @@ SIGNATURES = [
     ("umcx_gpu_forward_device", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, _P, C.POINTER(Result)]),
     ("umcx_gpu_rng_dump", C.c_int, [_P, C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32, C.c_uint32, _P]),
     ("umcx_measure_peaks", C.c_int, [C.c_int, C.POINTER(Peaks)]),
+    ("umcx_gpu_forward_noalloc", C.c_int, [C.c_int, C.POINTER(Sim), _P, _P, _P, _P, _P, _P, C.POINTER(Result)]),
     ("MCX_run_cmd", C.c_int, [C.POINTER(C.c_char_p), C.c_int]),
     ("MCX_run_json", C.c_int, [C.c_char_p]),
     ("umcx_main", C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),

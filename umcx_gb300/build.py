@@ -31,6 +31,7 @@ CU_UNITS = {
     "kernels_fast.cu": [],
     "kernels_strict.cu": ["--fmad=false"],
     "peaks.cu": [],
+    "noalloc.cu": [],
 }
 CPP_UNITS = ["jsonlite.cpp", "frontend.cpp", "run.cpp"]
 
