@@ -177,6 +177,69 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def measure_adjoint(ctx, args) -> dict:
+    """Forward + adjoint form (configuration 4: the configuration-1 grid and medium, 1e7 photons, four detectors,
+    50 gates): photons/ms of the adjoint forward kernel plus the backward pass (record reduction and replay of every
+    detected photon for the voxel Jacobians), device time."""
+    from umcx_gb300 import Job
+
+    cfg = json.loads(json.dumps(CONFIG))
+    cfg["Session"].update({"ID": "c4", "Photons": 10000000, "DoMismatch": 0})
+    cfg["Domain"]["Media"] = cfg["Domain"]["Media"][:2]
+    cfg["Shapes"] = cfg["Shapes"][:1]
+    job = Job.from_json(cfg)
+    sim = job.sim
+    fwd_ms, bwd_ms, recs = [], [], 0
+    for rep in range(3):
+        out = ctx.forward_adjoint(sim, job.labels, job.media, job.detpos)
+        adj = ctx.backward(jacobian=True)
+        if rep:
+            fwd_ms.append(out.result.kernel_ms)
+            bwd_ms.append(adj["replay_ms"])
+        recs = adj["records"]
+    f, b = statistics.mean(fwd_ms), statistics.mean(bwd_ms)
+    return {"workload": "configuration 1 grid/medium + 4 detectors, 50 gates, 1e7 photons; per-label mua/mus "
+                        "gradients of 200 detector readings and the summed volume + voxel Jacobians of 4 detectors",
+            "photons_per_ms": sim.nphoton / (f + b), "forward_adjoint_ms": f, "replay_ms": b,
+            "detected_records": int(recs), "replay_mismatch": int(adj["replay_mismatch"])}
+
+
+def measure_batched(ctx, args, device) -> dict:
+    """Batched form (configuration 5): 256 independent simulations in one persistent, graph-captured launch,
+    autotuned, versus the same simulations as sequential single launches on the same GPU."""
+    import torch
+
+    from umcx_gb300.api import Batch, autotune_batch
+    from umcx_gb300.workloads import batch5
+
+    jobs = batch5(args.batch_sims, photon_scale=args.batch_scale)
+    n = sum(j.sim.nphoton for j in jobs)
+    tune = autotune_batch(ctx, jobs, fraction=0.2, min_photons=500,
+                          candidates=((512, 1), (1024, 1), (512, 2), (1024, 2)))
+    b = Batch.from_jobs(ctx, jobs)
+    b.set_tuning(tune["block_size"], tune["blocks_per_sm"], tune["aggregation"])
+    b.run()
+    runs = [b.run() for _ in range(2)]
+    ms = statistics.mean(r.kernel_ms for r in runs)
+    steps_per_photon = runs[-1].steps / max(1, runs[-1].launched)
+    b.close()
+    # the same simulations one launch each (device buffers, same tuning)
+    ctx.set_tuning(tune["block_size"], tune["blocks_per_sm"], tune["aggregation"])
+    biggest = max(j.sim.dim[0] * j.sim.dim[1] * j.sim.dim[2] * j.sim.dim[3] for j in jobs)
+    d_flu = torch.empty(biggest, dtype=torch.float32, device=f"cuda:{device}")
+    stream = torch.cuda.current_stream()
+    seq = 0.0
+    for j in jobs:
+        d_lab = torch.from_numpy(j.labels.ravel().copy()).to(f"cuda:{device}")
+        seq += ctx.forward_device(j.sim, d_lab, j.media, None, d_flu, None, stream).kernel_ms
+    ctx.set_tuning()
+    return {"workload": f"{len(jobs)} simulations, edges 32-128, 2-5 labels, log-uniform 1e5-1e7 photons "
+                        f"(x{args.batch_scale}), 10 gates",
+            "photons": n, "steps_per_photon": steps_per_photon,
+            "photons_per_ms": n / ms, "graph_ms": ms, "sequential_photons_per_ms": n / seq,
+            "sequential_kernel_ms": seq, "speedup_vs_sequential": seq / ms, "tuning": tune}
+
+
 def run_gpu_arm(args) -> None:
     import numpy as np
     import torch
@@ -279,6 +342,10 @@ def run_gpu_arm(args) -> None:
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_reference_run(args.cpu_photons, os.cpu_count() or 1)
+    forms = {}
+    if rank == 0 and not args.no_forms:
+        forms["adjoint"] = measure_adjoint(ctx, args)
+        forms["batched"] = measure_batched(ctx, args, device)
 
     if rank == 0:
         line = {
@@ -312,6 +379,8 @@ def run_gpu_arm(args) -> None:
             line["cpu_baseline"] = {"value": cpu["value"], "unit": "photons/ms", "cores": os.cpu_count() or 1,
                                     "kind": cpu["kind"],
                                     "sample": f"{args.cpu_photons} photons of the same configuration"}
+        if forms:
+            line["forms"] = forms
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -332,6 +401,10 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--aggregation", type=int, default=0)
+    ap.add_argument("--no-forms", action="store_true", help="skip the adjoint and batched forms")
+    ap.add_argument("--batch-sims", type=int, default=256)
+    ap.add_argument("--batch-scale", type=float, default=0.01,
+                    help="photon-budget scale of the batched form (1.0 = the full 5.4e8-photon batch, ~4 min/run)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -114,7 +114,7 @@ typedef struct umcx_tuning {
     int32_t block_size;       /* threads per CTA */
     int32_t blocks_per_sm;    /* resident CTAs per SM for the persistent grid */
     int32_t aggregation;      /* 0 auto, 1 plain atomics, 2 warp match-any aggregation of fluence adds */
-    int32_t budget_ms;        /* wall-clock budget of one propagation launch; 0 = 600 000 ms.  When it runs out the
+    int32_t budget_ms;        /* wall-clock budget of one propagation launch; 0 = 300 000 ms.  When it runs out the
                                  kernel stops, the call returns UMCX_ERR_TIMEOUT and the context stays usable. */
 } umcx_tuning;
 
@@ -157,6 +157,69 @@ int umcx_gpu_forward(umcx_context* ctx, const umcx_sim* sim, const uint8_t* labe
  */
 int umcx_gpu_forward_device(umcx_context* ctx, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
                             const float* detpos, float* d_fluence, float* d_detp, void* stream, umcx_result* res);
+
+/*
+ * Differentiation (no counterpart in the reference, which has no adjoint and no photon replay).
+ *
+ * umcx_gpu_forward_adjoint runs the forward simulation (same inputs/outputs as umcx_gpu_forward) and additionally
+ * keeps, inside the context: one extended record per detected photon (photon index = its replay seed, detector,
+ * exit weight and time, path length and scatter count per label) and per-label tallies of the derivatives of the
+ * summed output volume.  umcx_gpu_backward then reduces them (FP64) into derivatives with respect to every label's
+ * mua and mus (per-voxel units, as in the media table), and optionally replays every detected photon from its seed
+ * to build the voxel-wise mua Jacobian of each detector.  Readings are raw sums of exit weights (divide by the
+ * launched photon count, or multiply by the normaliser, as needed); the time gate of a record is that of its exit
+ * time.
+ */
+typedef struct umcx_adjoint {
+    double* readings;        /* [detnum][maxgate]: sum of exit weights of detected photons, or NULL */
+    double* dread_dmua;      /* [detnum][maxgate][mediumnum], or NULL */
+    double* dread_dmus;      /* [detnum][maxgate][mediumnum], or NULL */
+    double* dflu_dmua;       /* [mediumnum]: derivative of the sum of the raw output volume, or NULL */
+    double* dflu_dmus;       /* [mediumnum], or NULL */
+    float* jacobian;         /* [detnum][nx][ny][nz]: d(sum over gates of readings)/d(mua of the voxel); NULL skips
+                                the replay */
+    uint64_t records;        /* out: detected-photon records used */
+    uint64_t replay_mismatch;/* out: replayed photons whose exit weight or detector differed from the record */
+    float replay_ms;         /* out: device time of the replay kernel */
+    int32_t reserved;
+} umcx_adjoint;
+
+int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* sim, const uint8_t* labels, const float* media,
+                             const float* detpos, float* fluence, float* detp, umcx_result* res);
+int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out);
+
+/*
+ * Batched simulations (no counterpart in the reference): many independent forward simulations -- different grid
+ * sizes, label counts, optics, sources and photon budgets -- run by one persistent kernel launch, replayed from a
+ * CUDA graph captured at creation.  Each simulation's photons are seeded exactly as in a single run of it, so every
+ * photon history, tally and output equals umcx_gpu_forward's for that simulation (up to the summation order of the
+ * output volume).  Detected-photon saving is not available in batches (issavedet must be 0).
+ *
+ * umcx_batch_create copies the host labels (uint8 [nx][ny][nz] each) and media tables, allocates the output pool and
+ * captures the graph (memsets, one or more kernel launches -- simulations are split into launches only when their
+ * descriptors and optical tables exceed a CTA's shared memory -- and the FP64-to-FP32 rounding).
+ */
+typedef struct umcx_batch umcx_batch;
+int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const uint8_t* const* labels,
+                      const float* const* media, umcx_batch** out);
+/* Run the whole batch once (graph launch + synchronise).  total receives the summed tallies and event counts and
+ * kernel_ms the device time of the graph. */
+int umcx_batch_run(umcx_batch* b, umcx_result* total);
+/* Copy simulation i's output volume of the last run to fluence (host, [maxgate][nx][ny][nz]); res receives its
+ * energy_escape / energy_total / launched (may be NULL). */
+int umcx_batch_get(umcx_batch* b, int i, float* fluence, umcx_result* res);
+/* Re-time the batch with the given tuning (NULL: defaults) and re-capture its graph. */
+int umcx_batch_set_tuning(umcx_batch* b, const umcx_tuning* tuning);
+void umcx_batch_destroy(umcx_batch* b);
+
+/*
+ * Autotuner (no reference counterpart): times short runs (sim's photons scaled by `fraction`, at least 20 000) of
+ * the forward kernel over block sizes, resident CTAs per SM and fluence-aggregation modes, keeps the fastest in
+ * *best and installs it on ctx.  Device buffers as for umcx_gpu_forward_device.
+ */
+int umcx_autotune(umcx_context* ctx, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
+                  const float* detpos, float* d_fluence, float* d_detp, double fraction, umcx_tuning* best,
+                  float* best_ms);
 
 /*
  * Debug known-answer hook for the random number generator (MCX_rand, L187-215): for photons

@@ -1,0 +1,80 @@
+"""Batched simulations (one persistent, graph-captured launch) against single runs of the same simulations (GPU).
+
+Every photon of simulation i is seeded exactly as in a single run of i, so photon histories are the same up to the
+last bits of single-precision arithmetic (the batched and single kernels are separate compilations, which may
+contract multiply-adds differently, so an occasional photon drifts by an ulp and then diverges): launched energy
+agrees exactly, escaped energy and output volumes to ~1e-6.  The single-run path itself is checked against the CPU
+oracle in test_forward_gpu.py."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(n=12, scale=0.02, max_edge=64):
+    from umcx_gb300.workloads import batch5
+
+    return batch5(n, photon_scale=scale, max_edge=max_edge)
+
+
+def test_batch_matches_single_runs(ctx):
+    from umcx_gb300.api import Batch
+
+    jobs = small_batch()
+    b = Batch.from_jobs(ctx, jobs)
+    tot = b.run()
+    assert tot.status == 0
+    assert tot.launched == sum(j.sim.nphoton for j in jobs)
+    for i, j in enumerate(jobs):
+        flu, r = b.get(i)
+        single = ctx.forward(j.sim, j.labels, j.media, j.detpos)
+        assert abs(r.energy_total - single.result.energy_total) <= 1e-9 * single.result.energy_total
+        assert abs(r.energy_escape - single.result.energy_escape) <= 1e-6 * single.result.energy_total
+        a, s = flu.astype(np.float64), single.fluence.astype(np.float64)
+        assert abs(a.sum() - s.sum()) <= 1e-5 * s.sum()
+        assert np.linalg.norm(a - s) <= 1e-3 * np.linalg.norm(s)
+    b.close()
+
+
+def test_batch_graph_replay_is_repeatable(ctx):
+    from umcx_gb300.api import Batch
+
+    jobs = small_batch(6, scale=0.01)
+    b = Batch.from_jobs(ctx, jobs)
+    r1 = b.run()
+    f1, _ = b.get(3)
+    r2 = b.run()
+    f2, _ = b.get(3)
+    assert (r1.steps, r1.crossings, r1.scatters) == (r2.steps, r2.crossings, r2.scatters)
+    np.testing.assert_allclose(f1, f2, rtol=1e-6, atol=1e-9)
+    b.set_tuning(256, 0, 2)  # re-captured with aggregation on
+    r3 = b.run()
+    assert r3.steps == r1.steps
+    b.close()
+
+
+def test_batch_rejects_detectors(ctx):
+    from umcx_gb300 import Job
+    from umcx_gb300.api import Batch
+
+    j = Job.from_args(["--bench", "cube60b", "-n", "1000"])
+    with pytest.raises(RuntimeError, match="detected photons"):
+        Batch.from_jobs(ctx, [j])
+
+
+def test_autotuners(ctx):
+    import torch
+
+    from umcx_gb300 import Job
+    from umcx_gb300.api import autotune_batch
+
+    job = Job.from_args(["--bench", "cubesph60b", "-n", "2e5"])
+    s = job.sim
+    d_lab = torch.from_numpy(job.labels.ravel().copy()).cuda()
+    d_flu = torch.zeros(s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3], dtype=torch.float32, device="cuda")
+    d_det = torch.zeros(s.maxdetphotons * 4, dtype=torch.float32, device="cuda")
+    best = ctx.autotune(s, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.2)
+    assert best["block_size"] in (128, 256, 512, 1024) and best["probe_ms"] > 0
+    ctx.set_tuning()
+    bb = autotune_batch(ctx, small_batch(4, scale=0.01), fraction=1.0, candidates=((256, 1), (512, 2)))
+    assert bb["block_size"] in (256, 512)

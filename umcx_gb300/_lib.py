@@ -86,6 +86,13 @@ class Peaks(C.Structure):
                 ("sm_count", C.c_int32), ("sm_clock_khz", C.c_int32)]
 
 
+class Adjoint(C.Structure):
+    _fields_ = [("readings", C.c_void_p), ("dread_dmua", C.c_void_p), ("dread_dmus", C.c_void_p),
+                ("dflu_dmua", C.c_void_p), ("dflu_dmus", C.c_void_p), ("jacobian", C.c_void_p),
+                ("records", C.c_uint64), ("replay_mismatch", C.c_uint64), ("replay_ms", C.c_float),
+                ("reserved", C.c_int32)]
+
+
 assert C.sizeof(Sim) == 168, C.sizeof(Sim)
 
 _P = C.c_void_p
@@ -103,6 +110,16 @@ SIGNATURES = [
     ("umcx_detp_columns", C.c_int, [C.POINTER(Sim)]),
     ("umcx_gpu_forward", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, C.POINTER(Result)]),
     ("umcx_gpu_forward_device", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, _P, C.POINTER(Result)]),
+    ("umcx_gpu_forward_adjoint", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, C.POINTER(Result)]),
+    ("umcx_gpu_backward", C.c_int, [_P, C.POINTER(Adjoint)]),
+    ("umcx_batch_create", C.c_int, [_P, C.c_int, C.POINTER(Sim), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                    C.POINTER(_P)]),
+    ("umcx_batch_run", C.c_int, [_P, C.POINTER(Result)]),
+    ("umcx_batch_get", C.c_int, [_P, C.c_int, _P, C.POINTER(Result)]),
+    ("umcx_batch_set_tuning", C.c_int, [_P, C.POINTER(Tuning)]),
+    ("umcx_batch_destroy", None, [_P]),
+    ("umcx_autotune", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, C.c_double, C.POINTER(Tuning),
+                                C.POINTER(C.c_float)]),
     ("umcx_gpu_rng_dump", C.c_int, [_P, C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32, C.c_uint32, _P]),
     ("umcx_measure_peaks", C.c_int, [C.c_int, C.POINTER(Peaks)]),
     ("umcx_gpu_forward_noalloc", C.c_int, [C.c_int, C.POINTER(Sim), _P, _P, _P, _P, _P, _P, C.POINTER(Result)]),

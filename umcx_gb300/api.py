@@ -214,6 +214,47 @@ class Context:
             dp = dp[: res.saved * cols].reshape(res.saved, cols)
         return Forward(flu, dp, res)
 
+    def forward_adjoint(self, sim: Sim, labels, media, detpos=None) -> Forward:
+        """Forward pass that keeps what umcx_gpu_backward needs (umcx_gpu_forward_adjoint)."""
+        lab = np.ascontiguousarray(labels, np.uint8)
+        med = np.ascontiguousarray(media, np.float32)
+        det = np.ascontiguousarray(detpos if detpos is not None else np.zeros((0, 4)), np.float32)
+        nout = sim.dim[0] * sim.dim[1] * sim.dim[2] * sim.dim[3]
+        flu = np.zeros(nout, np.float32) if sim.issavevol else None
+        cols = detp_columns(sim)
+        dp = np.zeros(max(1, sim.maxdetphotons * cols), np.float32) if sim.issavedet else None
+        res = Result()
+        rc = load().umcx_gpu_forward_adjoint(self._h, C.byref(sim), lab.ctypes.data, med.ctypes.data,
+                                             det.ctypes.data if det.size else None,
+                                             None if flu is None else flu.ctypes.data,
+                                             None if dp is None else dp.ctypes.data, C.byref(res))
+        check(rc, self._h, "umcx_gpu_forward_adjoint")
+        self._adj_sim = sim.copy()
+        if flu is not None:
+            flu = flu.reshape(sim.dim[3], sim.dim[0], sim.dim[1], sim.dim[2])
+        if dp is not None:
+            dp = dp[: res.saved * cols].reshape(res.saved, cols)
+        return Forward(flu, dp, res)
+
+    def backward(self, jacobian: bool = False) -> dict:
+        """Derivatives of the last forward_adjoint's detector readings and summed output (umcx_gpu_backward)."""
+        s = self._adj_sim
+        d, t, k = s.detnum, s.dim[3], s.mediumnum
+        out = {"readings": np.zeros((d, t)), "dread_dmua": np.zeros((d, t, k)), "dread_dmus": np.zeros((d, t, k)),
+               "dflu_dmua": np.zeros(k), "dflu_dmus": np.zeros(k)}
+        jac = np.zeros((d, s.dim[0], s.dim[1], s.dim[2]), np.float32) if jacobian and d else None
+        a = _lib.Adjoint()
+        a.readings = out["readings"].ctypes.data
+        a.dread_dmua = out["dread_dmua"].ctypes.data
+        a.dread_dmus = out["dread_dmus"].ctypes.data
+        a.dflu_dmua = out["dflu_dmua"].ctypes.data
+        a.dflu_dmus = out["dflu_dmus"].ctypes.data
+        a.jacobian = None if jac is None else jac.ctypes.data
+        check(load().umcx_gpu_backward(self._h, C.byref(a)), self._h, "umcx_gpu_backward")
+        out.update({"jacobian": jac, "records": a.records, "replay_mismatch": a.replay_mismatch,
+                    "replay_ms": a.replay_ms})
+        return out
+
     def forward_device(self, sim: Sim, d_labels, media, detpos, d_fluence, d_detp, stream=None) -> Result:
         """Device-buffer forward simulation (umcx_gpu_forward_device); d_* are torch CUDA tensors."""
         med = np.ascontiguousarray(media, np.float32)
@@ -228,9 +269,95 @@ class Context:
         check(rc, self._h, "umcx_gpu_forward_device")
         return res
 
+    def autotune(self, sim: Sim, d_labels, media, detpos, d_fluence, d_detp, fraction: float = 0.05) -> dict:
+        """Pick block size / CTAs per SM / aggregation for this simulation from short timed runs (umcx_autotune)."""
+        med = np.ascontiguousarray(media, np.float32)
+        det = np.ascontiguousarray(detpos if detpos is not None else np.zeros((0, 4)), np.float32)
+        best = Tuning()
+        ms = C.c_float()
+        rc = load().umcx_autotune(self._h, C.byref(sim), C.c_void_p(d_labels.data_ptr()), med.ctypes.data,
+                                  det.ctypes.data if det.size else None,
+                                  None if d_fluence is None else C.c_void_p(d_fluence.data_ptr()),
+                                  None if d_detp is None else C.c_void_p(d_detp.data_ptr()), float(fraction),
+                                  C.byref(best), C.byref(ms))
+        check(rc, self._h, "umcx_autotune")
+        return {"block_size": best.block_size, "blocks_per_sm": best.blocks_per_sm, "aggregation": best.aggregation,
+                "probe_ms": ms.value}
+
     def rng_dump(self, seeds, photon_offset: int, nphoton: int, ndraw: int) -> np.ndarray:
         s = (C.c_uint32 * 4)(*[int(x) for x in seeds])
         out = np.zeros(nphoton * ndraw, np.float32)
         check(load().umcx_gpu_rng_dump(self._h, s, int(photon_offset), int(nphoton), int(ndraw), out.ctypes.data),
               self._h, "umcx_gpu_rng_dump")
         return out.reshape(nphoton, ndraw)
+
+
+class Batch:
+    """Many independent simulations in one persistent, graph-captured launch (umcx_batch_*)."""
+
+    def __init__(self, ctx: Context, sims, labels, media):
+        lib = load()
+        n = len(sims)
+        arr = (Sim * n)(*[s.copy() for s in sims])
+        self._keep = [np.ascontiguousarray(x, np.uint8) for x in labels] + [np.ascontiguousarray(m, np.float32)
+                                                                            for m in media]
+        lab = (C.c_void_p * n)(*[x.ctypes.data for x in self._keep[:n]])
+        med = (C.c_void_p * n)(*[m.ctypes.data for m in self._keep[n:]])
+        self._ctx = ctx
+        self._h = C.c_void_p()
+        check(lib.umcx_batch_create(ctx.handle, n, arr, lab, med, C.byref(self._h)), ctx.handle, "umcx_batch_create")
+        self.sims = [s.copy() for s in sims]
+        self._keep = None
+
+    @classmethod
+    def from_jobs(cls, ctx: Context, jobs) -> "Batch":
+        return cls(ctx, [j.sim for j in jobs], [j.labels for j in jobs], [j.media for j in jobs])
+
+    def run(self) -> Result:
+        r = Result()
+        check(load().umcx_batch_run(self._h, C.byref(r)), self._ctx.handle, "umcx_batch_run")
+        return r
+
+    def get(self, i: int):
+        s = self.sims[i]
+        flu = np.zeros(s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3], np.float32) if s.issavevol else None
+        r = Result()
+        check(load().umcx_batch_get(self._h, int(i), None if flu is None else flu.ctypes.data, C.byref(r)),
+              self._ctx.handle, "umcx_batch_get")
+        if flu is not None:
+            flu = flu.reshape(s.dim[3], s.dim[0], s.dim[1], s.dim[2])
+        return flu, r
+
+    def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0, budget_ms: int = 0):
+        t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms)
+        check(load().umcx_batch_set_tuning(self._h, C.byref(t)), self._ctx.handle, "umcx_batch_set_tuning")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().umcx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def autotune_batch(ctx: Context, jobs, fraction: float = 0.05,
+                   candidates=((256, 1), (512, 1), (1024, 1), (256, 2), (512, 2), (1024, 2)),
+                   min_photons: int = 2000) -> dict:
+    """Autotuner for batches: times a photon-scaled copy of the batch for each (block size, aggregation) candidate
+    and returns the fastest configuration (apply it with Batch.set_tuning)."""
+    sims = []
+    for j in jobs:
+        s = j.sim
+        s.nphoton = min(s.nphoton, max(min_photons, int(s.nphoton * fraction)))
+        sims.append(s)
+    probe = Batch(ctx, sims, [j.labels for j in jobs], [j.media for j in jobs])
+    best = None
+    for block, agg in candidates:
+        probe.set_tuning(block, 0, agg)
+        probe.run()
+        ms = probe.run().kernel_ms
+        if best is None or ms < best["probe_ms"]:
+            best = {"block_size": block, "blocks_per_sm": 0, "aggregation": agg, "probe_ms": ms}
+    probe.close()
+    return best

@@ -30,6 +30,8 @@ CU_UNITS = {
     "capi.cu": [],
     "kernels_fast.cu": [],
     "kernels_strict.cu": ["--fmad=false"],
+    "kernels_adjoint.cu": [],
+    "kernels_batch.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],
 }

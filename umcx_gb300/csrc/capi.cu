@@ -10,6 +10,8 @@
 #include <exception>
 #include <new>
 #include <string>
+#include <vector>
+#include <algorithm>
 
 #include "../../include/umcx_gpu.h"
 #include "launch.h"
@@ -49,6 +51,12 @@ struct umcx_context {
     std::string err;
     umcx_tuning tuning{};
     DevBuf labels, fluence, detp, media, stats, counter, scratch, accum64;
+    // adjoint state kept between umcx_gpu_forward_adjoint and umcx_gpu_backward
+    DevBuf detrec, detext, grad, jac;
+    umcx_sim adj_sim{};
+    std::vector<float> adj_media, adj_det;
+    unsigned long long adj_records = 0;
+    bool adj_valid = false;
 };
 
 namespace {
@@ -158,7 +166,7 @@ KParams make_params(const umcx_sim* s, const float* detpos) {
     P.srcrdir = make_float4(1.f / s->srcdir[0], 1.f / s->srcdir[1], 1.f / s->srcdir[2], 0.f);
     P.srcparam1 = make_float4(s->srcparam1[0], s->srcparam1[1], s->srcparam1[2], s->srcparam1[3]);
     P.srcparam2 = make_float4(s->srcparam2[0], s->srcparam2[1], s->srcparam2[2], s->srcparam2[3]);
-    P.budget_ns = 600ULL * 1000000000ULL;  // 10 minutes
+    P.budget_ns = 300ULL * 1000000000ULL;  // 5 minutes (umcx_tuning.budget_ms overrides)
     for (int d = 0; d < s->detnum; d++)
         P.det[d] = make_float4(detpos[4 * d], detpos[4 * d + 1], detpos[4 * d + 2], detpos[4 * d + 3]);
     return P;
@@ -265,6 +273,7 @@ int umcx_create(umcx_context** out, int device) {
         UMCX_CK(cudaEventCreate(&ctx->ev1));
         UMCX_CK(configure_fast_kernels());
         UMCX_CK(configure_strict_kernels());
+        UMCX_CK(configure_adjoint_kernels());
         return UMCX_OK;
     });
     if (rc != UMCX_OK) {
@@ -287,6 +296,10 @@ void umcx_destroy(umcx_context* ctx) {
     ctx->counter.release();
     ctx->scratch.release();
     ctx->accum64.release();
+    ctx->detrec.release();
+    ctx->detext.release();
+    ctx->grad.release();
+    ctx->jac.release();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -391,6 +404,171 @@ int umcx_gpu_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* labels
     return rc;
 }
 
+int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t* labels, const float* media,
+                             const float* detpos, float* fluence, float* detp, umcx_result* res) {
+    if (!ctx) return UMCX_ERR_INPUT;
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = guarded(ctx, [&]() {
+        set_device(ctx);
+        validate(s);
+        if (!labels || !media) throw InputError("labels/media is NULL");
+        if (s->detnum > 0 && !detpos) throw InputError("detpos is NULL but detnum > 0");
+        if (s->flags & UMCX_SIM_STRICT_MATH) throw InputError("the adjoint runs the fast-math kernels only");
+        cudaStream_t st = ctx->stream;
+        const int K = s->mediumnum;
+        const size_t nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
+        const size_t nout = nvox * s->dim[3];
+        const int cols = umcx_detp_columns(s);
+        const unsigned long long cap = s->issavedet ? s->maxdetphotons : 0u;
+        UMCX_CK(ctx->labels.ensure(nvox));
+        UMCX_CK(cudaMemcpyAsync(ctx->labels.ptr, labels, nvox, cudaMemcpyHostToDevice, st));
+        if (s->issavevol) UMCX_CK(ctx->fluence.ensure(nout * sizeof(float)));
+        if (cap * cols) UMCX_CK(ctx->detp.ensure(cap * cols * sizeof(float)));
+        UMCX_CK(ctx->detrec.ensure((cap ? cap : 1) * sizeof(DetRecord)));
+        UMCX_CK(ctx->detext.ensure((cap ? cap : 1) * 2 * K * sizeof(float)));
+        UMCX_CK(ctx->grad.ensure(2 * K * sizeof(double)));
+        UMCX_CK(ctx->media.ensure(sizeof(Medium) * UMCX_MAX_MEDIA));
+        UMCX_CK(ctx->stats.ensure(sizeof(KStats)));
+        UMCX_CK(ctx->counter.ensure(sizeof(unsigned long long)));
+        KParams P = make_params(s, detpos);
+        P.maxdetphotons = static_cast<unsigned>(cap);
+        Medium hm[UMCX_MAX_MEDIA];
+        for (int i = 0; i < K; i++) hm[i] = make_medium(media + 4 * i);
+        UMCX_CK(cudaMemcpyAsync(ctx->media.ptr, hm, sizeof(Medium) * K, cudaMemcpyHostToDevice, st));
+        UMCX_CK(cudaMemsetAsync(ctx->stats.ptr, 0, sizeof(KStats), st));
+        UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), st));
+        UMCX_CK(cudaMemsetAsync(ctx->grad.ptr, 0, 2 * K * sizeof(double), st));
+        const bool fp64 = s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM);
+        if (fp64) {
+            UMCX_CK(ctx->accum64.ensure(nout * sizeof(double)));
+            UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, nout * sizeof(double), st));
+        } else if (s->issavevol) {
+            UMCX_CK(cudaMemsetAsync(ctx->fluence.ptr, 0, nout * sizeof(float), st));
+        }
+        KBuffers B;
+        std::memset(&B, 0, sizeof(B));
+        B.labels = static_cast<const uint8_t*>(ctx->labels.ptr);
+        B.fluence = s->issavevol ? static_cast<float*>(ctx->fluence.ptr) : nullptr;
+        B.fluence64 = fp64 ? static_cast<double*>(ctx->accum64.ptr) : nullptr;
+        B.detp = (cap * cols) ? static_cast<float*>(ctx->detp.ptr) : nullptr;
+        B.media = static_cast<const Medium*>(ctx->media.ptr);
+        B.stats = static_cast<KStats*>(ctx->stats.ptr);
+        B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
+        B.detrec = static_cast<DetRecord*>(ctx->detrec.ptr);
+        B.detext = static_cast<float*>(ctx->detext.ptr);
+        B.grad = static_cast<double*>(ctx->grad.ptr);
+        int block = ctx->tuning.block_size > 0 ? ctx->tuning.block_size : 256;
+        size_t smem = adjoint_smem(P, block);
+        while (smem > 227 * 1024 && block > 32) {
+            block /= 2;
+            smem = adjoint_smem(P, block);
+        }
+        if (smem > 227 * 1024) throw InputError("too many media for the adjoint's per-thread tallies");
+        int occ = adjoint_occupancy(s->isreflect != 0, block, smem);
+        if (occ < 1) occ = 1;
+        int grid = ctx->sm_count * occ;
+        const unsigned long long lanes = 1ULL * grid * block;
+        if (s->nphoton < lanes) grid = static_cast<int>(std::max<unsigned long long>(1ULL, (s->nphoton + block - 1) / block));
+        P.aggregate = 0;
+        if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
+        UMCX_CK(cudaEventRecord(ctx->ev0, st));
+        launch_adjoint(grid, block, smem, s->isreflect != 0, P, B, st);
+        UMCX_CK(cudaGetLastError());
+        UMCX_CK(cudaEventRecord(ctx->ev1, st));
+        if (fp64) {
+            launch_fp64_to_fp32(static_cast<const double*>(ctx->accum64.ptr), static_cast<float*>(ctx->fluence.ptr), nout,
+                                ctx->sm_count, st);
+            UMCX_CK(cudaGetLastError());
+        }
+        umcx_result tmp;
+        umcx_result* r = res ? res : &tmp;
+        collect(ctx, s, st, r);
+        if (s->issavevol && fluence)
+            UMCX_CK(cudaMemcpyAsync(fluence, ctx->fluence.ptr, nout * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (cap * cols && detp && r->saved)
+            UMCX_CK(cudaMemcpyAsync(detp, ctx->detp.ptr, r->saved * cols * sizeof(float), cudaMemcpyDeviceToHost, st));
+        UMCX_CK(cudaStreamSynchronize(st));
+        ctx->adj_sim = *s;
+        ctx->adj_media.assign(media, media + 4 * K);
+        ctx->adj_det.assign(detpos ? detpos : media, detpos ? detpos + 4 * s->detnum : media);
+        ctx->adj_records = r->saved;
+        ctx->adj_valid = true;
+        return UMCX_OK;
+    });
+    if (res) {
+        res->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        res->status = rc;
+    }
+    return rc;
+}
+
+int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out) {
+    if (!ctx) return UMCX_ERR_INPUT;
+    return guarded(ctx, [&]() {
+        if (!out) throw InputError("out is NULL");
+        if (!ctx->adj_valid) throw InputError("umcx_gpu_backward needs a preceding umcx_gpu_forward_adjoint");
+        set_device(ctx);
+        cudaStream_t st = ctx->stream;
+        const umcx_sim* s = &ctx->adj_sim;
+        const int K = s->mediumnum;
+        const size_t nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
+        const size_t ncell = static_cast<size_t>(s->detnum) * s->dim[3];
+        KParams P = make_params(s, ctx->adj_det.data());
+        const unsigned long long n = ctx->adj_records;
+        // detector readings and derivatives
+        const size_t rbytes = ncell * sizeof(double), gbytes = ncell * K * sizeof(double);
+        UMCX_CK(ctx->scratch.ensure(rbytes + 2 * gbytes + 64));
+        double* d_read = static_cast<double*>(ctx->scratch.ptr);
+        double* d_gmua = d_read + ncell;
+        double* d_gmus = d_gmua + ncell * K;
+        UMCX_CK(cudaMemsetAsync(d_read, 0, rbytes + 2 * gbytes, st));
+        launch_adjoint_reduce(P, static_cast<const DetRecord*>(ctx->detrec.ptr), static_cast<const float*>(ctx->detext.ptr),
+                              n, static_cast<const Medium*>(ctx->media.ptr), d_read, d_gmua, d_gmus, ctx->sm_count, st);
+        UMCX_CK(cudaGetLastError());
+        if (out->readings) UMCX_CK(cudaMemcpyAsync(out->readings, d_read, rbytes, cudaMemcpyDeviceToHost, st));
+        if (out->dread_dmua) UMCX_CK(cudaMemcpyAsync(out->dread_dmua, d_gmua, gbytes, cudaMemcpyDeviceToHost, st));
+        if (out->dread_dmus) UMCX_CK(cudaMemcpyAsync(out->dread_dmus, d_gmus, gbytes, cudaMemcpyDeviceToHost, st));
+        const double* g = static_cast<const double*>(ctx->grad.ptr);
+        if (out->dflu_dmua) UMCX_CK(cudaMemcpyAsync(out->dflu_dmua, g, K * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (out->dflu_dmus) UMCX_CK(cudaMemcpyAsync(out->dflu_dmus, g + K, K * sizeof(double), cudaMemcpyDeviceToHost, st));
+        out->records = n;
+        out->replay_mismatch = 0;
+        out->replay_ms = 0.f;
+        if (out->jacobian && s->detnum > 0) {
+            const size_t jbytes = static_cast<size_t>(s->detnum) * nvox * sizeof(float);
+            UMCX_CK(ctx->jac.ensure(jbytes));
+            UMCX_CK(cudaMemsetAsync(ctx->jac.ptr, 0, jbytes, st));
+            UMCX_CK(cudaMemsetAsync(ctx->stats.ptr, 0, sizeof(KStats), st));
+            UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), st));
+            KBuffers B;
+            std::memset(&B, 0, sizeof(B));
+            B.labels = static_cast<const uint8_t*>(ctx->labels.ptr);
+            B.media = static_cast<const Medium*>(ctx->media.ptr);
+            B.stats = static_cast<KStats*>(ctx->stats.ptr);
+            B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
+            B.replay_list = static_cast<const DetRecord*>(ctx->detrec.ptr);
+            B.replay_count = n;
+            B.jacobian = static_cast<float*>(ctx->jac.ptr);
+            const int block = 128;
+            int grid = static_cast<int>(std::min<unsigned long long>((n + block - 1) / block, 8ULL * ctx->sm_count));
+            if (grid < 1) grid = 1;
+            UMCX_CK(cudaEventRecord(ctx->ev0, st));
+            launch_replay(grid, block, s->isreflect != 0, P, B, st);
+            UMCX_CK(cudaGetLastError());
+            UMCX_CK(cudaEventRecord(ctx->ev1, st));
+            KStats stats;
+            UMCX_CK(cudaMemcpyAsync(&stats, ctx->stats.ptr, sizeof(stats), cudaMemcpyDeviceToHost, st));
+            UMCX_CK(cudaMemcpyAsync(out->jacobian, ctx->jac.ptr, jbytes, cudaMemcpyDeviceToHost, st));
+            UMCX_CK(cudaStreamSynchronize(st));
+            UMCX_CK(cudaEventElapsedTime(&out->replay_ms, ctx->ev0, ctx->ev1));
+            out->replay_mismatch = stats.capped;
+            if (stats.error) throw BudgetError("replay kernel stopped at its wall-clock budget");
+        }
+        UMCX_CK(cudaStreamSynchronize(st));
+        return UMCX_OK;
+    });
+}
+
 int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photon_offset, uint32_t nphoton,
                       uint32_t ndraw, float* out) {
     if (!ctx) return UMCX_ERR_INPUT;
@@ -408,6 +586,399 @@ int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photo
         UMCX_CK(cudaStreamSynchronize(ctx->stream));
         return UMCX_OK;
     });
+}
+
+int umcx_autotune(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labels, const float* media,
+                  const float* detpos, float* d_fluence, float* d_detp, double fraction, umcx_tuning* best,
+                  float* best_ms) {
+    if (!ctx) return UMCX_ERR_INPUT;
+    return guarded(ctx, [&]() {
+        validate(s);
+        set_device(ctx);
+        if (!(fraction > 0.0) || fraction > 1.0) throw InputError("fraction must be in (0, 1]");
+        umcx_sim probe = *s;
+        const double n = static_cast<double>(s->nphoton) * fraction;
+        probe.nphoton = static_cast<uint64_t>(n < 20000.0 ? 20000.0 : n);
+        if (probe.nphoton > s->nphoton) probe.nphoton = s->nphoton;
+        const umcx_tuning saved = ctx->tuning;
+        umcx_tuning keep = saved;
+        float keep_ms = 1e30f;
+        const int blocks[] = {128, 256, 512, 1024};
+        for (int agg = 1; agg <= 2; agg++) {
+            for (int bs : blocks) {
+                umcx_tuning t = saved;
+                t.block_size = bs;
+                t.blocks_per_sm = 0;
+                t.aggregation = agg;
+                ctx->tuning = t;
+                float ms = 0.f;
+                for (int rep = 0; rep < 2; rep++) {  // first run warms up, second is timed
+                    umcx_result r;
+                    enqueue_forward(ctx, &probe, d_labels, media, detpos, d_fluence, d_detp, ctx->stream);
+                    collect(ctx, &probe, ctx->stream, &r);
+                    ms = r.kernel_ms;
+                }
+                if (ms < keep_ms) {
+                    keep_ms = ms;
+                    keep = t;
+                }
+            }
+        }
+        ctx->tuning = keep;
+        if (best) *best = keep;
+        if (best_ms) *best_ms = keep_ms;
+        return UMCX_OK;
+    });
+}
+
+}  // extern "C"
+
+// ================================================================================================= batches
+struct umcx_batch {
+    umcx_context* ctx = nullptr;
+    int nsim = 0;
+    std::vector<umcx_sim> sims;
+    std::vector<unsigned long long> out_off;
+    unsigned long long nout_total = 0;
+    bool reflect = false, fp64 = true;
+    struct Chunk {
+        int first = 0, count = 0, media_first = 0, total_media = 0;
+        unsigned long long photons = 0, begin_off = 0;
+        int block = 0, grid = 0;
+        size_t smem = 0;
+    };
+    std::vector<Chunk> chunks;
+    std::vector<SimDesc> descs;
+    DevBuf labels, media, d_descs, d_begin, tallies, out32, out64, counters, stats;
+    cudaGraphExec_t exec = nullptr;
+    umcx_tuning tuning{};
+    std::vector<double> host_tallies;
+};
+
+namespace {
+
+constexpr size_t kBatchSmemBudget = 200 * 1024;
+
+void batch_plan(umcx_batch* b) {
+    for (auto& ch : b->chunks) {
+        const int block = b->tuning.block_size > 0 ? b->tuning.block_size : 512;
+        const size_t smem = batch_smem(ch.count, ch.total_media, block);
+        if (smem > 227 * 1024) throw InputError("batch chunk does not fit shared memory at this block size");
+        int occ = batch_occupancy(b->reflect, block, smem);
+        if (occ < 1) occ = 1;
+        const int per_sm = b->tuning.blocks_per_sm > 0 ? std::min(b->tuning.blocks_per_sm, occ) : occ;
+        int grid = b->ctx->sm_count * per_sm;
+        if (ch.photons < 1ULL * grid * block)
+            grid = static_cast<int>(std::max<unsigned long long>(1ULL, (ch.photons + block - 1) / block));
+        ch.block = block;
+        ch.grid = grid;
+        ch.smem = smem;
+    }
+}
+
+// enqueue one full batch run on the context stream (used inside the graph capture)
+void batch_enqueue(umcx_batch* b, cudaStream_t st) {
+    UMCX_CK(cudaMemsetAsync(b->stats.ptr, 0, sizeof(KStats), st));
+    UMCX_CK(cudaMemsetAsync(b->counters.ptr, 0, sizeof(unsigned long long) * b->chunks.size(), st));
+    UMCX_CK(cudaMemsetAsync(b->tallies.ptr, 0, sizeof(double) * 2 * b->nsim, st));
+    if (b->fp64) UMCX_CK(cudaMemsetAsync(b->out64.ptr, 0, sizeof(double) * b->nout_total, st));
+    else UMCX_CK(cudaMemsetAsync(b->out32.ptr, 0, sizeof(float) * b->nout_total, st));
+    for (size_t c = 0; c < b->chunks.size(); c++) {
+        const auto& ch = b->chunks[c];
+        BParams bp;
+        std::memset(&bp, 0, sizeof(bp));
+        bp.sims = static_cast<const SimDesc*>(b->d_descs.ptr) + ch.first;
+        bp.begin = static_cast<const unsigned long long*>(b->d_begin.ptr) + ch.begin_off;
+        bp.tallies = static_cast<double*>(b->tallies.ptr) + 2 * ch.first;
+        bp.nsim = ch.count;
+        bp.total_media = ch.total_media;
+        bp.aggregate = b->tuning.aggregation == 2 ? 1 : 0;
+        bp.total = ch.photons;
+        bp.budget_ns = b->tuning.budget_ms > 0 ? static_cast<unsigned long long>(b->tuning.budget_ms) * 1000000ULL
+                                               : 300ULL * 1000000000ULL;
+        KBuffers B;
+        std::memset(&B, 0, sizeof(B));
+        B.labels = static_cast<const uint8_t*>(b->labels.ptr);
+        B.fluence = static_cast<float*>(b->out32.ptr);
+        B.fluence64 = b->fp64 ? static_cast<double*>(b->out64.ptr) : nullptr;
+        B.media = static_cast<const Medium*>(b->media.ptr) + ch.media_first;
+        B.stats = static_cast<KStats*>(b->stats.ptr);
+        B.counter = static_cast<unsigned long long*>(b->counters.ptr) + c;
+        launch_batch(ch.grid, ch.block, ch.smem, b->reflect, bp, B, st);
+        UMCX_CK(cudaGetLastError());
+    }
+    if (b->fp64) {
+        launch_fp64_to_fp32(static_cast<const double*>(b->out64.ptr), static_cast<float*>(b->out32.ptr), b->nout_total,
+                            b->ctx->sm_count, st);
+        UMCX_CK(cudaGetLastError());
+    }
+}
+
+void batch_capture(umcx_batch* b) {
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    batch_plan(b);
+    cudaStream_t st = b->ctx->stream;
+    UMCX_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        batch_enqueue(b, st);
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    cudaGraph_t graph = nullptr;
+    UMCX_CK(cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    UMCX_CK(e);
+}
+
+SimDesc make_desc(const umcx_sim* s, unsigned media_base, unsigned long long label_off, unsigned long long out_off) {
+    const KParams P = make_params(s, nullptr);
+    SimDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.nx = P.nx;
+    d.ny = P.ny;
+    d.nz = P.nz;
+    d.maxgate = P.maxgate;
+    d.dimyz = P.dimyz;
+    d.dimxyz = P.dimxyz;
+    d.isreflect = P.isreflect;
+    d.issavevol = P.issavevol;
+    d.outputtype = P.outputtype;
+    d.srctype = P.srctype;
+    d.step_cap = P.step_cap;
+    d.media_base = media_base;
+    d.tstart = P.tstart;
+    d.tend = P.tend;
+    d.rtstep = P.rtstep;
+    d.unitinmm = P.unitinmm;
+    for (int k = 0; k < 4; k++) d.seeds[k] = P.seeds[k];
+    d.label_off = label_off;
+    d.out_off = out_off;
+    d.photon_offset = s->photon_offset;
+    d.nphoton = s->nphoton;
+    d.srcpos = P.srcpos;
+    d.srcdir = P.srcdir;
+    d.srcrdir = P.srcrdir;
+    d.srcparam1 = P.srcparam1;
+    d.srcparam2 = P.srcparam2;
+    return d;
+}
+
+// upload the begin (prefix) arrays of every chunk for photon counts `counts` (one per simulation)
+void batch_upload_begin(umcx_batch* b, const std::vector<unsigned long long>& counts, DevBuf& dst,
+                        std::vector<unsigned long long>* chunk_totals) {
+    std::vector<unsigned long long> begin;
+    if (chunk_totals) chunk_totals->clear();
+    for (auto& ch : b->chunks) {
+        unsigned long long acc = 0;
+        for (int i = 0; i < ch.count; i++) {
+            begin.push_back(acc);
+            acc += counts[static_cast<size_t>(ch.first + i)];
+        }
+        begin.push_back(acc);
+        if (chunk_totals) chunk_totals->push_back(acc);
+    }
+    UMCX_CK(dst.ensure(begin.size() * sizeof(unsigned long long)));
+    UMCX_CK(cudaMemcpy(dst.ptr, begin.data(), begin.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
+extern "C" {
+
+int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const uint8_t* const* labels,
+                      const float* const* media, umcx_batch** out) {
+    if (!ctx || !out) return UMCX_ERR_INPUT;
+    *out = nullptr;
+    umcx_batch* b = new (std::nothrow) umcx_batch();
+    if (!b) return UMCX_ERR_INPUT;
+    b->ctx = ctx;
+    int rc = guarded(ctx, [&]() {
+        if (nsim < 1 || !sims || !labels || !media) throw InputError("empty batch or NULL arrays");
+        set_device(ctx);
+        UMCX_CK(configure_batch_kernels());
+        b->nsim = nsim;
+        b->sims.assign(sims, sims + nsim);
+        std::vector<Medium> table;
+        std::vector<unsigned long long> label_off(static_cast<size_t>(nsim)), media_first(static_cast<size_t>(nsim));
+        unsigned long long lab_total = 0;
+        b->out_off.resize(static_cast<size_t>(nsim));
+        b->fp64 = false;
+        for (int i = 0; i < nsim; i++) {
+            const umcx_sim* s = &sims[i];
+            validate(s);
+            if (s->issavedet) throw InputError("simulation " + std::to_string(i) + ": batches do not save detected photons");
+            if (s->flags & UMCX_SIM_STRICT_MATH) throw InputError("batches run the fast-math kernel only");
+            if (!labels[i] || !media[i]) throw InputError("simulation " + std::to_string(i) + ": NULL labels or media");
+            const unsigned long long nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
+            label_off[static_cast<size_t>(i)] = lab_total;
+            lab_total += (nvox + 15) & ~15ULL;
+            b->out_off[static_cast<size_t>(i)] = b->nout_total;
+            b->nout_total += s->issavevol ? nvox * s->dim[3] : 0;
+            media_first[static_cast<size_t>(i)] = table.size();
+            for (int m = 0; m < s->mediumnum; m++) table.push_back(make_medium(media[i] + 4 * m));
+            if (s->isreflect) b->reflect = true;
+            if (s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM)) b->fp64 = true;
+        }
+        // chunks: as many consecutive simulations as fit a CTA's shared memory at block 1024
+        int first = 0;
+        while (first < nsim) {
+            umcx_batch::Chunk ch;
+            ch.first = first;
+            ch.media_first = static_cast<int>(media_first[static_cast<size_t>(first)]);
+            int count = 0, tm = 0;
+            while (first + count < nsim) {
+                const int m = sims[first + count].mediumnum;
+                if (count > 0 && batch_smem(count + 1, tm + m, 1024) > kBatchSmemBudget) break;
+                tm += m;
+                count++;
+            }
+            ch.count = count;
+            ch.total_media = tm;
+            b->chunks.push_back(ch);
+            first += count;
+        }
+        // descriptors (media_base relative to the chunk's first medium)
+        b->descs.resize(static_cast<size_t>(nsim));
+        for (auto& ch : b->chunks)
+            for (int i = ch.first; i < ch.first + ch.count; i++)
+                b->descs[static_cast<size_t>(i)] =
+                    make_desc(&sims[i], static_cast<unsigned>(media_first[static_cast<size_t>(i)] - ch.media_first),
+                              label_off[static_cast<size_t>(i)], b->out_off[static_cast<size_t>(i)]);
+        std::vector<unsigned long long> counts(static_cast<size_t>(nsim)), totals;
+        for (int i = 0; i < nsim; i++) counts[static_cast<size_t>(i)] = sims[i].nphoton;
+        unsigned long long boff = 0;
+        for (auto& ch : b->chunks) {
+            ch.begin_off = boff;
+            boff += static_cast<unsigned long long>(ch.count) + 1;
+        }
+        batch_upload_begin(b, counts, b->d_begin, &totals);
+        for (size_t c = 0; c < b->chunks.size(); c++) b->chunks[c].photons = totals[c];
+        // device buffers
+        UMCX_CK(b->labels.ensure(lab_total));
+        for (int i = 0; i < nsim; i++) {
+            const unsigned long long nvox = 1ULL * sims[i].dim[0] * sims[i].dim[1] * sims[i].dim[2];
+            UMCX_CK(cudaMemcpy(static_cast<uint8_t*>(b->labels.ptr) + label_off[static_cast<size_t>(i)], labels[i], nvox,
+                               cudaMemcpyHostToDevice));
+        }
+        UMCX_CK(b->media.ensure(table.size() * sizeof(Medium)));
+        UMCX_CK(cudaMemcpy(b->media.ptr, table.data(), table.size() * sizeof(Medium), cudaMemcpyHostToDevice));
+        UMCX_CK(b->d_descs.ensure(b->descs.size() * sizeof(SimDesc)));
+        UMCX_CK(cudaMemcpy(b->d_descs.ptr, b->descs.data(), b->descs.size() * sizeof(SimDesc), cudaMemcpyHostToDevice));
+        UMCX_CK(b->tallies.ensure(sizeof(double) * 2 * nsim));
+        UMCX_CK(b->out32.ensure(sizeof(float) * (b->nout_total ? b->nout_total : 1)));
+        if (b->fp64) UMCX_CK(b->out64.ensure(sizeof(double) * (b->nout_total ? b->nout_total : 1)));
+        UMCX_CK(b->counters.ensure(sizeof(unsigned long long) * b->chunks.size()));
+        UMCX_CK(b->stats.ensure(sizeof(KStats)));
+        b->tuning = ctx->tuning;
+        batch_capture(b);
+        return UMCX_OK;
+    });
+    if (rc != UMCX_OK) {
+        umcx_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return UMCX_OK;
+}
+
+int umcx_batch_run(umcx_batch* b, umcx_result* total) {
+    if (!b) return UMCX_ERR_INPUT;
+    umcx_context* ctx = b->ctx;
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = guarded(ctx, [&]() {
+        set_device(ctx);
+        cudaStream_t st = ctx->stream;
+        UMCX_CK(cudaEventRecord(ctx->ev0, st));
+        UMCX_CK(cudaGraphLaunch(b->exec, st));
+        UMCX_CK(cudaEventRecord(ctx->ev1, st));
+        KStats stats;
+        b->host_tallies.resize(static_cast<size_t>(2 * b->nsim));
+        UMCX_CK(cudaMemcpyAsync(&stats, b->stats.ptr, sizeof(stats), cudaMemcpyDeviceToHost, st));
+        UMCX_CK(cudaMemcpyAsync(b->host_tallies.data(), b->tallies.ptr, sizeof(double) * 2 * b->nsim,
+                                cudaMemcpyDeviceToHost, st));
+        UMCX_CK(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        UMCX_CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        if (total) {
+            std::memset(total, 0, sizeof(*total));
+            for (int i = 0; i < b->nsim; i++) {
+                total->energy_escape += b->host_tallies[static_cast<size_t>(2 * i)];
+                total->energy_total += b->host_tallies[static_cast<size_t>(2 * i + 1)];
+            }
+            total->launched = stats.launched;
+            total->steps = stats.steps;
+            total->crossings = stats.crossings;
+            total->scatters = stats.scatters;
+            total->reflections = stats.reflections;
+            total->capped = stats.capped;
+            total->kernel_ms = ms;
+            total->status = stats.error ? UMCX_ERR_TIMEOUT : UMCX_OK;
+        }
+        if (stats.error) throw BudgetError("batched kernel stopped at its wall-clock budget; results are partial");
+        return UMCX_OK;
+    });
+    if (total) {
+        total->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        total->status = rc;
+    }
+    return rc;
+}
+
+int umcx_batch_get(umcx_batch* b, int i, float* fluence, umcx_result* res) {
+    if (!b) return UMCX_ERR_INPUT;
+    return guarded(b->ctx, [&]() {
+        if (i < 0 || i >= b->nsim) throw InputError("simulation index out of range");
+        set_device(b->ctx);
+        const umcx_sim& s = b->sims[static_cast<size_t>(i)];
+        if (fluence && s.issavevol) {
+            const size_t n = 1ULL * s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3];
+            UMCX_CK(cudaMemcpy(fluence, static_cast<float*>(b->out32.ptr) + b->out_off[static_cast<size_t>(i)],
+                               n * sizeof(float), cudaMemcpyDeviceToHost));
+        }
+        if (res) {
+            std::memset(res, 0, sizeof(*res));
+            if (b->host_tallies.size() == static_cast<size_t>(2 * b->nsim)) {
+                res->energy_escape = b->host_tallies[static_cast<size_t>(2 * i)];
+                res->energy_total = b->host_tallies[static_cast<size_t>(2 * i + 1)];
+            }
+            res->launched = s.nphoton;
+        }
+        return UMCX_OK;
+    });
+}
+
+int umcx_batch_set_tuning(umcx_batch* b, const umcx_tuning* t) {
+    if (!b) return UMCX_ERR_INPUT;
+    return guarded(b->ctx, [&]() {
+        set_device(b->ctx);
+        if (t) b->tuning = *t;
+        else std::memset(&b->tuning, 0, sizeof(b->tuning));
+        batch_capture(b);
+        return UMCX_OK;
+    });
+}
+
+void umcx_batch_destroy(umcx_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->labels.release();
+    b->media.release();
+    b->d_descs.release();
+    b->d_begin.release();
+    b->tallies.release();
+    b->out32.release();
+    b->out64.release();
+    b->counters.release();
+    b->stats.release();
+    delete b;
 }
 
 }  // extern "C"

@@ -9,7 +9,6 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
-#include <functional>
 #include <sstream>
 #include <stdexcept>
 
@@ -302,54 +301,143 @@ void UserIO::benchmark(const std::string& name) {
 struct P3 {
     float x, y, z;
 };
-static float jnum(const Value& o, const char* key, size_t i) { return o.at(key).at(i).as_float(); }
 
-// label of one shape at a voxel centre; 0 = not inside (the reference returns int quiet_NaN, i.e. 0)
-using ShapeFn = std::function<int(const P3&, const Value&)>;
-
-static int shape_sphere(const P3& p, const Value& o) {
-    const float ox = jnum(o, "O", 0), oy = jnum(o, "O", 1), oz = jnum(o, "O", 2), r = o.at("R").as_float();
-    return ((p.x - ox) * (p.x - ox) + (p.y - oy) * (p.y - oy) + (p.z - oz) * (p.z - oz) < (r * r)) ? o.at("Tag").as_int()
-                                                                                                    : 0;
+// A shape construct compiled once into plain floats; evaluated per voxel centre with the reference's float
+// expressions (L458-473).  A missing key throws where the reference's lookup would: for a value that every voxel
+// reads, at the first voxel; for one read only inside the shape (the tag, the Box extent), at the first voxel that
+// reaches it.  0 = not inside (the reference returns int quiet_NaN, i.e. 0).
+struct OptF {
+    float v = 0.f;
+    bool ok = false;
+};
+static OptF opt_num(const Value& o, const char* key, size_t i) {
+    OptF r;
+    const Value* a = o.find(key);
+    if (a && a->is_array() && i < a->size() && a->at(i).is_number()) {
+        r.v = a->at(i).as_float();
+        r.ok = true;
+    }
+    return r;
 }
-// The reference's Box reads a key spelled "Sip.ze" and compares p.x three times (L460); once a voxel centre passes
-// the origin test it evaluates that missing key, which throws.  The same behaviour is kept.
-static int shape_box(const P3& p, const Value& o) {
-    const float ox = jnum(o, "O", 0), oy = jnum(o, "O", 1), oz = jnum(o, "O", 2);
-    if (p.x < ox || p.y < oy || p.z < oz) return 0;
-    const Value* sz = o.find("Sip.ze");
-    if (!sz) throw js::type_error("type must be number, but is null");
-    bool outside = p.x > ox + sz->at(0).as_float() || p.x > oy + sz->at(1).as_float() || p.x > oz + sz->at(2).as_float();
-    return !outside ? o.at("Tag").as_int() : 0;
+static OptF opt_scalar(const Value& v) {
+    OptF r;
+    if (v.is_number() || v.is_bool()) {
+        r.v = v.as_float();
+        r.ok = true;
+    }
+    return r;
 }
-static int shape_xlayer(const P3& p, const Value& o) {
-    return (p.x >= o.at(0).as_float() && p.x <= o.at(1).as_float()) ? o.at(2).as_int() : 0;
-}
-static int shape_ylayer(const P3& p, const Value& o) {
-    return (p.y >= o.at(0).as_float() && p.y <= o.at(1).as_float()) ? o.at(2).as_int() : 0;
-}
-static int shape_zlayer(const P3& p, const Value& o) {
-    return (p.z >= o.at(0).as_float() && p.z <= o.at(1).as_float()) ? o.at(2).as_int() : 0;
-}
-static int shape_cylinder(const P3& p, const Value& o) {
-    const float ax = jnum(o, "C1", 0) - jnum(o, "C0", 0), ay = jnum(o, "C1", 1) - jnum(o, "C0", 1),
-                az = jnum(o, "C1", 2) - jnum(o, "C0", 2);
-    const float d0 = ax * ax + ay * ay + az * az;
-    const float vx = ax / sqrtf(d0), vy = ay / sqrtf(d0), vz = az / sqrtf(d0);
-    const float px = p.x - jnum(o, "C0", 0), py = p.y - jnum(o, "C0", 1), pz = p.z - jnum(o, "C0", 2);
-    const float d = vx * px + vy * py + vz * pz;
-    const float r = o.at("R").as_float();
-    // the axial bound compares the projection with the SQUARED axis length (L469)
-    return (d <= d0 && d >= 0.f && px * px + py * py + pz * pz - d * d <= r * r) ? o.at("Tag").as_int() : 0;
+[[noreturn]] static void missing_number() { throw js::type_error("type must be number, but is null"); }
+static float need(const OptF& f) {
+    if (!f.ok) missing_number();
+    return f.v;
 }
 
-static const ShapeFn* find_shape(const std::string& key) {
-    static const std::pair<const char*, ShapeFn> table[] = {
-        {"Sphere", shape_sphere},   {"Box", shape_box},           {"XLayers", shape_xlayer},
-        {"YLayers", shape_ylayer},  {"ZLayers", shape_zlayer},    {"Cylinder", shape_cylinder}};
-    for (const auto& e : table)
-        if (key == e.first) return &e.second;
-    return nullptr;
+struct CompiledShape {
+    enum Kind { kSphere, kBox, kXLayers, kYLayers, kZLayers, kCylinder } kind = kSphere;
+    float o[3] = {0, 0, 0}, r = 0;                     // sphere / box origin, radius
+    OptF boxsize[3];                                   // Box: the "Sip.ze" key the reference reads
+    float ax = 0, ay = 0, az = 0, d0 = 0, vx = 0, vy = 0, vz = 0, c0[3] = {0, 0, 0};  // cylinder
+    int tag = 0;
+    bool tag_ok = false;
+    struct Layer {
+        OptF lo, hi;
+        int tag = 0;
+        bool tag_ok = false;
+    };
+    std::vector<Layer> layers;
+};
+
+static bool compile_shape(const std::string& key, const Value& body, CompiledShape* cs) {
+    auto read_tag = [&](const Value& v, int* tag, bool* ok) {
+        const Value* t = v.find("Tag");
+        *ok = t && (t->is_number() || t->is_bool());
+        *tag = *ok ? t->as_int() : 0;
+    };
+    if (key == "Sphere") {
+        cs->kind = CompiledShape::kSphere;
+        for (int k = 0; k < 3; k++) cs->o[k] = need(opt_num(body, "O", static_cast<size_t>(k)));
+        cs->r = need(opt_scalar(body.contains("R") ? body.at("R") : Value()));
+        read_tag(body, &cs->tag, &cs->tag_ok);
+    } else if (key == "Box") {
+        // the reference reads a key spelled "Sip.ze" and compares p.x three times (L460)
+        cs->kind = CompiledShape::kBox;
+        for (int k = 0; k < 3; k++) cs->o[k] = need(opt_num(body, "O", static_cast<size_t>(k)));
+        for (int k = 0; k < 3; k++) cs->boxsize[k] = opt_num(body, "Sip.ze", static_cast<size_t>(k));
+        read_tag(body, &cs->tag, &cs->tag_ok);
+    } else if (key == "XLayers" || key == "YLayers" || key == "ZLayers") {
+        cs->kind = key[0] == 'X' ? CompiledShape::kXLayers : (key[0] == 'Y' ? CompiledShape::kYLayers : CompiledShape::kZLayers);
+        for (const Value& layer : body.items()) {
+            CompiledShape::Layer L;
+            if (!layer.is_array()) missing_number();
+            L.lo = layer.size() > 0 ? opt_scalar(layer.at(0)) : OptF();
+            L.hi = layer.size() > 1 ? opt_scalar(layer.at(1)) : OptF();
+            if (layer.size() > 2 && (layer.at(2).is_number() || layer.at(2).is_bool())) {
+                L.tag = layer.at(2).as_int();
+                L.tag_ok = true;
+            }
+            need(L.lo);
+            cs->layers.push_back(L);
+        }
+    } else if (key == "Cylinder") {
+        cs->kind = CompiledShape::kCylinder;
+        float c1[3];
+        for (int k = 0; k < 3; k++) {
+            cs->c0[k] = need(opt_num(body, "C0", static_cast<size_t>(k)));
+            c1[k] = need(opt_num(body, "C1", static_cast<size_t>(k)));
+        }
+        cs->ax = c1[0] - cs->c0[0];
+        cs->ay = c1[1] - cs->c0[1];
+        cs->az = c1[2] - cs->c0[2];
+        cs->d0 = cs->ax * cs->ax + cs->ay * cs->ay + cs->az * cs->az;
+        cs->vx = cs->ax / sqrtf(cs->d0);
+        cs->vy = cs->ay / sqrtf(cs->d0);
+        cs->vz = cs->az / sqrtf(cs->d0);
+        cs->r = need(opt_scalar(body.contains("R") ? body.at("R") : Value()));
+        read_tag(body, &cs->tag, &cs->tag_ok);
+    } else {
+        return false;
+    }
+    return true;
+}
+
+static int inside_tag(int tag, bool ok) {
+    if (!ok) missing_number();
+    return tag;
+}
+
+// label painted by one shape at voxel centre p (0 = none)
+static int eval_shape(const CompiledShape& cs, const P3& p, size_t layer) {
+    switch (cs.kind) {
+        case CompiledShape::kSphere:
+            return ((p.x - cs.o[0]) * (p.x - cs.o[0]) + (p.y - cs.o[1]) * (p.y - cs.o[1]) +
+                        (p.z - cs.o[2]) * (p.z - cs.o[2]) <
+                    (cs.r * cs.r))
+                       ? inside_tag(cs.tag, cs.tag_ok)
+                       : 0;
+        case CompiledShape::kBox: {
+            if (p.x < cs.o[0] || p.y < cs.o[1] || p.z < cs.o[2]) return 0;
+            const bool outside = p.x > cs.o[0] + need(cs.boxsize[0]) || p.x > cs.o[1] + need(cs.boxsize[1]) ||
+                                 p.x > cs.o[2] + need(cs.boxsize[2]);
+            return !outside ? inside_tag(cs.tag, cs.tag_ok) : 0;
+        }
+        case CompiledShape::kXLayers:
+        case CompiledShape::kYLayers:
+        case CompiledShape::kZLayers: {
+            const CompiledShape::Layer& L = cs.layers[layer];
+            const float c = cs.kind == CompiledShape::kXLayers ? p.x : (cs.kind == CompiledShape::kYLayers ? p.y : p.z);
+            return (c >= L.lo.v && c <= need(L.hi)) ? inside_tag(L.tag, L.tag_ok) : 0;
+        }
+        case CompiledShape::kCylinder: {
+            const float px = p.x - cs.c0[0], py = p.y - cs.c0[1], pz = p.z - cs.c0[2];
+            const float d = cs.vx * px + cs.vy * py + cs.vz * pz;
+            // the axial bound compares the projection with the SQUARED axis length (L469)
+            return (d <= cs.d0 && d >= 0.f && px * px + py * py + pz * pz - d * d <= cs.r * cs.r)
+                       ? inside_tag(cs.tag, cs.tag_ok)
+                       : 0;
+        }
+    }
+    return 0;
 }
 
 std::vector<unsigned char> base64_decode(const std::string& in) {
@@ -440,23 +528,18 @@ void UserIO::initdomain() {
             }
             for (const Value* obj : objs) {
                 const std::string key = obj->is_object() && !obj->empty() ? obj->front_member().first : std::string();
-                const ShapeFn* fn = find_shape(key);
-                if (fn) {
-                    const Value& body = obj->front_member().second;
+                CompiledShape cs;
+                if (compile_shape(key, obj->front_member().second, &cs)) {
                     const bool layers = key.find("Layers") == 1;
+                    const size_t nl = layers ? cs.layers.size() : 1;
                     for (uint32_t z = 0; z < domain.nz; z++)
                         for (uint32_t y = 0; y < domain.ny; y++)
                             for (uint32_t x = 0; x < domain.nx; x++) {
                                 const int64_t idx = domain.index(static_cast<int>(x), static_cast<int>(y), static_cast<int>(z));
                                 const P3 p{x + 0.5f, y + 0.5f, z + 0.5f};
-                                if (layers) {
-                                    for (const Value& layer : body.items()) {
-                                        int label = (*fn)(p, layer);
-                                        if (label) domain.vol[static_cast<size_t>(idx)] = label;  // MCX_volume::mask, L138-140
-                                    }
-                                } else {
-                                    int label = (*fn)(p, body);
-                                    if (label) domain.vol[static_cast<size_t>(idx)] = label;
+                                for (size_t l = 0; l < nl; l++) {
+                                    const int label = eval_shape(cs, p, l);
+                                    if (label) domain.vol[static_cast<size_t>(idx)] = label;  // MCX_volume::mask, L138-140
                                 }
                             }
                 } else if (!(key == "Name" || key == "Grid" || key == "Origin")) {

@@ -1,0 +1,30 @@
+// kernels_batch.cu - instances of the batched propagation kernel.
+#include "launch.h"
+
+namespace umcx_dev {
+
+size_t batch_smem(int nsim, int total_media, int block) {
+    return sizeof(SimDesc) * static_cast<size_t>(nsim) + sizeof(unsigned long long) * static_cast<size_t>((nsim + 2) & ~1) +
+           sizeof(Medium) * static_cast<size_t>(total_media) + sizeof(float) * static_cast<size_t>(block);
+}
+
+cudaError_t configure_batch_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    return e;
+}
+
+int batch_occupancy(bool reflect, int block, size_t smem) {
+    int n = 0;
+    cudaError_t e = reflect ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<true>, block, smem)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<false>, block, smem);
+    return e == cudaSuccess ? n : 0;
+}
+
+void launch_batch(int grid, int block, size_t smem, bool reflect, const BParams& BP, const KBuffers& B,
+                  cudaStream_t st) {
+    if (reflect) k_batch<true><<<grid, block, smem, st>>>(BP, B);
+    else k_batch<false><<<grid, block, smem, st>>>(BP, B);
+}
+
+}  // namespace umcx_dev

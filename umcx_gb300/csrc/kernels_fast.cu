@@ -52,7 +52,9 @@ void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B,
 }
 
 size_t forward_smem(const KParams& P, int block, bool savedet) {
-    size_t s = sizeof(Medium) * static_cast<size_t>(P.mediumnum);
+    size_t s = 2 * sizeof(double) * static_cast<size_t>(block);  // per-lane energy tallies
+    s += sizeof(Medium) * static_cast<size_t>(P.mediumnum);
+    s += sizeof(float) * static_cast<size_t>(block);  // per-lane launch weight
     if (savedet) s += sizeof(float) * static_cast<size_t>(P.ppathlen) * static_cast<size_t>(block);
     s += sizeof(float) * static_cast<size_t>(block);  // aggregation buffer
     return s;

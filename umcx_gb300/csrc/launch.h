@@ -34,6 +34,24 @@ cudaError_t configure_fast_kernels();
 cudaError_t configure_strict_kernels();
 int occupancy_strict(bool reflect, bool savedet, int block, size_t smem);
 
+// adjoint forward pass, replay and record reduction (kernels_adjoint.cu)
+size_t adjoint_smem(const KParams& P, int block);
+cudaError_t configure_adjoint_kernels();
+int adjoint_occupancy(bool reflect, int block, size_t smem);
+void launch_adjoint(int grid, int block, size_t smem, bool reflect, const KParams& P, const KBuffers& B,
+                    cudaStream_t st);
+void launch_replay(int grid, int block, bool reflect, const KParams& P, const KBuffers& B, cudaStream_t st);
+void launch_adjoint_reduce(const KParams& P, const DetRecord* rec, const float* ext, unsigned long long n,
+                           const Medium* media, double* read, double* gmua, double* gmus, int sm_count,
+                           cudaStream_t st);
+
+// batched simulations (kernels_batch.cu)
+size_t batch_smem(int nsim, int total_media, int block);
+cudaError_t configure_batch_kernels();
+int batch_occupancy(bool reflect, int block, size_t smem);
+void launch_batch(int grid, int block, size_t smem, bool reflect, const BParams& BP, const KBuffers& B,
+                  cudaStream_t st);
+
 void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream);
 
 void launch_rng_dump(const uint32_t seeds[4], unsigned long long offset, unsigned nphoton, unsigned ndraw, float* out,

@@ -169,7 +169,10 @@ struct Photon {
     Rng rng;
 };
 
-__device__ __forceinline__ int vox_index(const KParams& P, int ix, int iy, int iz) {  // L128-130
+// The engine functions below are templates over the parameter view PV: KParams (one simulation, kernel
+// parameter) or SimDesc (one simulation of a batch, shared memory); both expose the same member names.
+template <class PV>
+__device__ __forceinline__ int vox_index(const PV& P, int ix, int iy, int iz) {  // L128-130
     return (ix < 0 || iy < 0 || iz < 0 || ix >= P.nx || iy >= P.ny || iz >= P.nz)
                ? -1
                : static_cast<int>(static_cast<unsigned>(ix) * P.dimyz + static_cast<unsigned>(iy) * static_cast<unsigned>(P.nz) +
@@ -198,8 +201,8 @@ __device__ __forceinline__ void rotate(Photon& p, float stheta, float ctheta, fl
 }
 
 // MCX_photon::launch, L225-259; returns the launch weight
-template <bool STRICT>
-__device__ __forceinline__ float launch(const KParams& P, Photon& p, unsigned long long i) {
+template <bool STRICT, class PV>
+__device__ __forceinline__ float launch(const PV& P, Photon& p, unsigned long long i) {
     const unsigned i32 = static_cast<unsigned>(i);
     rng_reseed(p.rng, P.seeds[0] ^ i32, P.seeds[1] | i32, P.seeds[2] ^ i32, P.seeds[3] | i32);  // L761
     p.px = P.srcpos.x;
@@ -286,7 +289,8 @@ __device__ __forceinline__ float launch(const KParams& P, Photon& p, unsigned lo
 }
 
 // MCX_photon::skip, L339-358: moves a photon launched outside the grid to its entry point; false if it misses
-__device__ __forceinline__ bool skip_to_grid(const KParams& P, Photon& p) {
+template <class PV>
+__device__ __forceinline__ bool skip_to_grid(const PV& P, Photon& p) {
     const float ax = -p.px * p.rx, ay = -p.py * p.ry, az = -p.pz * p.rz;
     const float bx = (static_cast<float>(P.nx) - p.px) * p.rx;
     const float by = (static_cast<float>(P.ny) - p.py) * p.ry;
@@ -312,8 +316,8 @@ __device__ __forceinline__ bool skip_to_grid(const KParams& P, Photon& p) {
 
 // MCX_photon::step, L315-338; returns the new voxel index (lastvox when the step ends inside the voxel).
 // *seg returns the distance moved.
-template <bool STRICT>
-__device__ __forceinline__ int step(const KParams& P, Photon& p, const Medium& m, bool* crossed) {
+template <bool STRICT, class PV>
+__device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, bool* crossed) {
     const float hx = fabsf((static_cast<float>(p.ix + (p.vx > 0.f)) - p.px) * p.rx);
     const float hy = fabsf((static_cast<float>(p.iy + (p.vy > 0.f)) - p.py) * p.ry);
     const float hz = fabsf((static_cast<float>(p.iz + (p.vz > 0.f)) - p.pz) * p.rz);
@@ -450,8 +454,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // deposit value of MCX_photon::save (L359-363)
-template <bool STRICT>
-__device__ __forceinline__ float deposit_value(const KParams& P, const Photon& p, const Medium& m) {
+template <bool STRICT, class PV>
+__device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, const Medium& m) {
     if (P.outputtype == UMCX_OUT_ENERGY) return p.lw - p.pw;
     if (m.a.x < FLT_EPSILON) return p.lw * p.lz;
     if constexpr (STRICT) return (p.lw - p.pw) / m.a.x;
@@ -467,189 +471,672 @@ __device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v)
 
 __global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n);
 
-// =============================================================================================== the kernel
-// Shared memory layout: Medium[mediumnum] | float ppath[ppathlen][blockDim] | float aggbuf[blockDim] (aggregation)
+// =============================================================================================== loop building blocks
+struct Counters {
+    unsigned launch = 0, steps = 0, cross = 0, scat = 0, refl = 0, cap = 0;
+};
+
+// what one loop iteration did to an active photon
+struct Event {
+    bool crossed;        // a voxel boundary was crossed: a deposit site (L285)
+    bool term;           // the photon terminated
+    bool scattered;      // a scattering event happened, in medium scat_mid
+    int left_vox;        // voxel left at the crossing
+    unsigned left_mid;   // its medium
+    int gate;            // time gate of the deposit (negative before tstart)
+    float seg;           // path since the previous deposit site (len.z before the reset)
+    float w_before;      // weight at the previous deposit site (len.w before the reset)
+    float dep_val;       // the value MCX_photon::save deposits (L360)
+    unsigned scat_mid;
+};
+
+// L761-762 + L262-271: seed photon idx, launch it, move it onto the grid; false when it misses the grid
+template <bool STRICT, class PV>
+__device__ __forceinline__ bool start_photon(const PV& P, const uint8_t* __restrict__ labels, Photon& p,
+                                             unsigned long long idx) {
+    p.launchw = launch<STRICT>(P, p, idx);
+    p.lastvox = vox_index(P, p.ix, p.iy, p.iz);
+    const bool inside = p.lastvox >= 0 || skip_to_grid(P, p);
+    if (inside) {
+        p.media = __ldg(labels + p.lastvox);
+        p.lx = scat_len<STRICT>(p.rng);
+    } else {
+        p.media = 0;
+    }
+    return inside;
+}
+
+// One iteration for an active photon: a voxel step and, at a voxel change, the deposit bookkeeping, time-gate test,
+// boundary handling and label update of MCX_photon::sprint (L281-314); then a scatter when the free path is used up
+// (L272-274).  Every kernel (forward, adjoint, replay) advances photons with this one function, so a replayed photon
+// follows the forward pass's trajectory.  RESET_SEGMENT resets the deposit segment at every crossing even when no
+// volume is saved (per-voxel path lengths for the adjoint and the replay); trajectories do not depend on it.
+template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV>
+__device__ __forceinline__ void advance(const PV& P, const uint8_t* __restrict__ labels, const Medium* sm,
+                                        Photon& p, Event& ev, Counters& c) {
+    ev.crossed = false;
+    ev.term = false;
+    ev.scattered = false;
+    if (p.lx > 0.f) {
+        const unsigned mid = p.media & UMCX_LABEL_MASK;
+        const Medium m = sm[mid];
+        bool crossed;
+        int newvox = step<STRICT>(P, p, m, &crossed);
+        c.steps++;
+        if (++p.nsteps > P.step_cap) {
+            ev.term = true;
+            c.cap++;
+        } else if (newvox != p.lastvox) {
+            c.cross++;
+            ev.crossed = true;
+            ev.left_vox = p.lastvox;
+            ev.left_mid = mid;
+            ev.seg = p.lz;
+            ev.w_before = p.lw;
+            ev.gate = static_cast<int>(fminf(static_cast<float>(P.maxgate - 1),
+                                             static_cast<float>(static_cast<int>(floorf((p.ly - P.tstart) * P.rtstep)))));
+            ev.dep_val = deposit_value<STRICT>(P, p, m);
+            if (RESET_SEGMENT || P.issavevol) {
+                p.lw = p.pw;
+                p.lz = 0.f;
+            }
+            if (p.ly > P.tend) {
+                ev.term = true;
+            } else {
+                unsigned newmedia = (newvox >= 0) ? __ldg(labels + newvox) : 0u;
+                const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
+                if (REFLECT && P.isreflect && m.a.w != n2) {
+                    c.refl++;
+                    if (reflect<STRICT>(p, m.a.w, n2)) {
+                        if (newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0) ev.term = true;
+                    } else {
+                        newvox = p.lastvox;
+                        newmedia = p.media;
+                    }
+                } else if (newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0)) {
+                    ev.term = true;
+                }
+                if (!ev.term) {
+                    p.lastvox = newvox;
+                    p.media = newmedia;
+                }
+            }
+        }
+    }
+    if (!ev.term && p.lx <= 0.f) {
+        ev.scattered = true;
+        ev.scat_mid = p.media & UMCX_LABEL_MASK;
+        scatter<STRICT>(p, sm[ev.scat_mid]);
+        c.scat++;
+    }
+}
+
+// per-lane photon indices: the first is the lane's global index, the next one is fetched from the global counter
+// when the current one starts, so the atomic's latency overlaps the photon's whole life
+// (indices [0, lanes) are the lanes' first photons; counter value c stands for photon lanes + c)
+struct PhotonFeed {
+    unsigned long long next;
+    __device__ __forceinline__ void init(unsigned long long* counter, unsigned long long gid, unsigned long long total,
+                                         unsigned long long lanes) {
+        (void)counter;
+        (void)total;
+        (void)lanes;
+        next = gid;
+    }
+    // false when no photon is left; otherwise returns the prefetched index and prefetches the following one
+    __device__ __forceinline__ bool take(unsigned long long* counter, unsigned long long* idx, unsigned long long n) {
+        if (next >= n) return false;
+        *idx = next;
+        next = atomicAdd(counter, 1ULL) + static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+        return true;
+    }
+};
+
+__device__ __forceinline__ bool det_hit(const float4 dp, const Photon& p) {  // L430-431
+    return (dp.x - p.px) * (dp.x - p.px) + (dp.y - p.py) * (dp.y - p.py) + (dp.z - p.pz) * (dp.z - p.pz) < dp.w * dp.w;
+}
+
+// fluence deposit of one iteration, called by all lanes of the warp (converged)
+__device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggregate, float* aggbuf, unsigned tid,
+                                                  unsigned lane, int dep_idx, float dep_val) {
+    if (aggregate) {
+        const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
+        if (__popc(hm) > 1) {
+            const unsigned grp = __match_any_sync(kFull, dep_idx >= 0 ? static_cast<unsigned>(dep_idx) : 0xFFFFFFFFu);
+            aggbuf[tid] = dep_val;
+            __syncwarp();
+            if (dep_idx >= 0 && lane == __ffs(grp) - 1u) {
+                float s = 0.f;
+                const unsigned base = tid & ~31u;
+                for (unsigned g = grp; g; g &= g - 1) s += aggbuf[base + __ffs(g) - 1];
+                deposit_add(B, dep_idx, s);
+            }
+            __syncwarp();
+            return;
+        }
+    }
+    if (dep_idx >= 0) deposit_add(B, dep_idx, dep_val);
+}
+
+// detected-photon append (L276-278, L429-435; MCX_detect::addphoton L164-176), called by all lanes (converged):
+// per detector a ballot, one atomic per warp, a prefix count for the slot.  Returns (through *slots) the slot
+// taken for each detector hit so callers can write extra per-record data.
+template <class WriteRecord>
+__device__ __forceinline__ void detect_converged(const KParams& P, const KBuffers& B, unsigned lane, bool tdet,
+                                                 const Photon& p, WriteRecord&& write) {
+    if (!__any_sync(kFull, tdet)) return;
+    for (int d = 0; d < P.detnum; d++) {
+        const bool hit = tdet && det_hit(P.det[d], p);
+        const unsigned hm = __ballot_sync(kFull, hit);
+        if (hm == 0u) continue;
+        const unsigned leader = __ffs(hm) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&B.stats->detected, static_cast<unsigned long long>(__popc(hm)));
+        base = __shfl_sync(kFull, base, leader);
+        if (hit) {
+            const unsigned long long slot = base + __popc(hm & ((1u << lane) - 1u));
+            if (slot < P.maxdetphotons) write(d, slot);
+        }
+    }
+}
+
+// the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction]
+__device__ __forceinline__ void write_detp(const KParams& P, const KBuffers& B, const Photon& p, const float* ppath,
+                                           unsigned stride, int d, unsigned long long slot) {
+    float* rec = B.detp + slot * static_cast<unsigned long long>(P.cols);
+    int k = 0;
+    if (P.savedetflag & UMCX_DET_ID) rec[k++] = static_cast<float>(d + 1);
+    if (P.savedetflag & UMCX_DET_PPATH)
+        for (int q = 0; q < P.ppathlen; q++) rec[k++] = ppath[q * stride];
+    if (P.savedetflag & UMCX_DET_EXITPOS) {
+        rec[k++] = p.px;
+        rec[k++] = p.py;
+        rec[k++] = p.pz;
+    }
+    if (P.savedetflag & UMCX_DET_EXITDIR) {
+        rec[k++] = p.vx;
+        rec[k++] = p.vy;
+        rec[k++] = p.vz;
+    }
+}
+
+// per-warp reduction of the lane tallies, one set of atomics per warp
+__device__ __forceinline__ void flush_tallies(const KBuffers& B, unsigned lane, double tot, double esc, Counters c) {
+    for (int off = 16; off > 0; off >>= 1) {
+        tot += __shfl_down_sync(kFull, tot, off);
+        esc += __shfl_down_sync(kFull, esc, off);
+        c.launch += __shfl_down_sync(kFull, c.launch, off);
+        c.steps += __shfl_down_sync(kFull, c.steps, off);
+        c.cross += __shfl_down_sync(kFull, c.cross, off);
+        c.scat += __shfl_down_sync(kFull, c.scat, off);
+        c.refl += __shfl_down_sync(kFull, c.refl, off);
+        c.cap += __shfl_down_sync(kFull, c.cap, off);
+    }
+    if (lane == 0) {
+        atomicAdd(&B.stats->total, tot);
+        atomicAdd(&B.stats->escape, esc);
+        atomicAdd(&B.stats->launched, static_cast<unsigned long long>(c.launch));
+        atomicAdd(&B.stats->steps, static_cast<unsigned long long>(c.steps));
+        atomicAdd(&B.stats->crossings, static_cast<unsigned long long>(c.cross));
+        atomicAdd(&B.stats->scatters, static_cast<unsigned long long>(c.scat));
+        atomicAdd(&B.stats->reflections, static_cast<unsigned long long>(c.refl));
+        if (c.cap) atomicAdd(&B.stats->capped, static_cast<unsigned long long>(c.cap));
+    }
+}
+
+// copies the media table (3 float4 per medium) into shared memory
+__device__ __forceinline__ void load_media(const KParams& P, const Medium* src, Medium* sm) {
+    const float4* s = reinterpret_cast<const float4*>(src);
+    float4* d = reinterpret_cast<float4*>(sm);
+    for (int k = threadIdx.x; k < 3 * P.mediumnum; k += blockDim.x) d[k] = s[k];
+    __syncthreads();
+}
+
+// uniform exit of a warp when the launch's wall-clock budget is used up
+__device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, unsigned lane,
+                                              unsigned long long t_end) {
+    if ((iter & 1023u) != 0u) return false;
+    const bool late = global_ns() > t_end;
+    if (__any_sync(kFull, late)) {
+        if (lane == 0) atomicExch(&B.stats->error, UMCX_ERR_TIMEOUT);
+        return true;
+    }
+    return false;
+}
+
+// =============================================================================================== forward kernel
+// Shared memory: Medium[mediumnum] | float ppath[ppathlen][blockDim] | float aggbuf[blockDim]
 template <bool STRICT, bool REFLECT, bool SAVEDET>
 __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
-    Medium* sm = reinterpret_cast<Medium*>(smem4);
+    // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
+    // them out of the register budget of the hot loop
+    double* tally = reinterpret_cast<double*>(smem4);  // [2][blockDim]: total, escape
+    Medium* sm = reinterpret_cast<Medium*>(tally + 2 * blockDim.x);
     float* ppath = reinterpret_cast<float*>(sm + P.mediumnum);
     float* aggbuf = ppath + (SAVEDET ? P.ppathlen * blockDim.x : 0);
-    {
-        const float4* src = reinterpret_cast<const float4*>(B.media);
-        float4* dst = reinterpret_cast<float4*>(sm);
-        for (int k = threadIdx.x; k < 3 * P.mediumnum; k += blockDim.x) dst[k] = src[k];
-    }
-    __syncthreads();
+    float* lwbuf = aggbuf + blockDim.x;
+    load_media(P, B.media, sm);
 
     const unsigned tid = threadIdx.x;
     const unsigned lane = lane_id();
-    const unsigned long long nthreads = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
-    const unsigned long long gid = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + tid;
-    const unsigned long long N = P.nphoton;
+    tally[tid] = 0.0;
+    tally[blockDim.x + tid] = 0.0;
+    PhotonFeed feed;
+    feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + tid, P.nphoton,
+              static_cast<unsigned long long>(gridDim.x) * blockDim.x);
+    const unsigned long long t_end = global_ns() + P.budget_ns;
+    Photon p;
+    p.media = 0;
+    p.lastvox = -1;
+    bool active = false, done = false;
+    Counters c;
 
-    // the first photon of a lane is its global thread index; later ones come from the counter (offset by nthreads)
-    unsigned long long next = gid;
-    unsigned long long pending = (gid < N) ? atomicAdd(B.counter, 1ULL) + nthreads : N;
+    for (unsigned iter = 0;; iter++) {
+        if (!active && !done) {  // launch a photon on an idle lane (L761-763)
+            unsigned long long k;
+            if (!feed.take(B.counter, &k, P.nphoton)) {
+                done = true;
+            } else {
+                c.launch++;
+                active = start_photon<STRICT>(P, B.labels, p, P.photon_offset + k);
+                lwbuf[tid] = p.launchw;
+                if (SAVEDET && active)
+                    for (int q = 0; q < P.ppathlen; q++) ppath[q * blockDim.x + tid] = 0.f;
+            }
+        }
+        if (__all_sync(kFull, done)) break;
+        if (out_of_budget(B, iter, lane, t_end)) break;
 
+        int dep_idx = -1;
+        float dep_val = 0.f;
+        Event ev;
+        ev.term = false;
+        if (active) {
+            advance<STRICT, REFLECT, false>(P, B.labels, sm, p, ev, c);
+            if (ev.crossed) {
+                if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.left_mid > 0)
+                    ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
+                if (P.issavevol && ev.gate >= 0) {
+                    dep_idx = ev.left_vox + ev.gate * static_cast<int>(P.dimxyz);
+                    dep_val = ev.dep_val;
+                }
+            }
+        }
+        deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
+        if (SAVEDET) {
+            const bool tdet = ev.term && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
+            detect_converged(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
+                write_detp(P, B, p, ppath + tid, blockDim.x, d, slot);
+            });
+        }
+        if (ev.term) {  // energy tallies (L765-770)
+            if ((p.media & UMCX_LABEL_MASK) != 0u) {
+                tally[tid] += static_cast<double>(lwbuf[tid]);
+                tally[blockDim.x + tid] += static_cast<double>(p.pw);
+            }
+            active = false;
+        }
+    }
+    flush_tallies(B, lane, tally[tid], tally[blockDim.x + tid], c);
+}
+
+// =============================================================================================== adjoint kernel
+// The forward pass of the adjoint: the forward kernel's outputs plus, per photon, the tallies that make the
+// derivatives of the summed output volume with respect to every label's mua and mus, and an extended record per
+// detected photon (photon index, detector, exit weight and time, path and scatter count per label).
+//
+// Fluence derivatives (F_j = deposit j, in label m_j, segment length l_j, L_k(<j) / n_k(<=j) = path / scatters in
+// label k before deposit j, S = running sum of F):
+//   dSum/dmua_k = -sum_j L_k(<j) F_j + sum_{j: m_j = k} dF_j/dmua_k|path
+//               = -(L_k S - Q_k) + E_k            with Q_k += l_j S (after adding F_j), E_k += dF_j/dmua
+//   dSum/dmus_k = sum_j F_j (n_k(<=j)/mus_k - L_k(<=j))           (score of the path prefix up to deposit j)
+//               = (cnt_k S - R_k)/mus_k - (L_k S - Q_k + T_k)   with R_k += S at each scatter, T_k += F_j l_j
+// so each deposit and each scatter updates one label's tallies (O(1) per event).
+//
+// Shared memory: double ga[K][bd], gs[K][bd] | Medium[K] | float ppath[ppathlen][bd] | float L, cnt, Q, T, E, R[K][bd]
+template <bool REFLECT>
+__global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffers B) {
+    extern __shared__ double smem8[];
+    const unsigned bd = blockDim.x;
+    const int K = P.mediumnum;
+    double* ga = smem8;
+    double* gs = ga + K * bd;
+    Medium* sm = reinterpret_cast<Medium*>(gs + K * bd);
+    float* ppath = reinterpret_cast<float*>(sm + K);
+    float* Lk = ppath + P.ppathlen * bd;
+    float* Ck = Lk + K * bd;
+    float* Qk = Ck + K * bd;
+    float* Tk = Qk + K * bd;
+    float* Ek = Tk + K * bd;
+    float* Rk = Ek + K * bd;
+    load_media(P, B.media, sm);
+
+    const unsigned tid = threadIdx.x;
+    const unsigned lane = lane_id();
+    for (int k = 0; k < K; k++) {
+        ga[k * bd + tid] = 0.0;
+        gs[k * bd + tid] = 0.0;
+    }
+    PhotonFeed feed;
+    feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * bd + tid, P.nphoton,
+              static_cast<unsigned long long>(gridDim.x) * bd);
     const unsigned long long t_end = global_ns() + P.budget_ns;
     Photon p;
     p.media = 0;
     p.lastvox = -1;
     bool active = false, done = false;
     double tot = 0.0, esc = 0.0;
-    unsigned c_launch = 0, c_steps = 0, c_cross = 0, c_scat = 0, c_refl = 0, c_cap = 0;
+    Counters c;
+    float S = 0.f;
+    unsigned long long cur = 0;
 
     for (unsigned iter = 0;; iter++) {
-        // ---- launch a photon on an idle lane (L761-763)
         if (!active && !done) {
-            if (next >= N) {
+            unsigned long long k;
+            if (!feed.take(B.counter, &k, P.nphoton)) {
                 done = true;
             } else {
-                const unsigned long long idx = P.photon_offset + next;
-                next = pending;
-                pending = (next < N) ? atomicAdd(B.counter, 1ULL) + nthreads : N;
-                p.launchw = launch<STRICT>(P, p, idx);
-                c_launch++;
-                p.lastvox = vox_index(P, p.ix, p.iy, p.iz);
-                bool inside = p.lastvox >= 0 || skip_to_grid(P, p);  // L263-267
-                if (inside) {
-                    p.media = __ldg(B.labels + p.lastvox);
-                    p.lx = scat_len<STRICT>(p.rng);
-                    if (SAVEDET)
-                        for (int k = 0; k < P.ppathlen; k++) ppath[k * blockDim.x + tid] = 0.f;
-                    active = true;
+                c.launch++;
+                cur = P.photon_offset + k;
+                active = start_photon<false>(P, B.labels, p, cur);
+                if (active) {
+                    S = 0.f;
+                    for (int q = 0; q < P.ppathlen; q++) ppath[q * bd + tid] = 0.f;
+                    for (int q = 0; q < K; q++) {
+                        Lk[q * bd + tid] = 0.f;
+                        Ck[q * bd + tid] = 0.f;
+                        Qk[q * bd + tid] = 0.f;
+                        Tk[q * bd + tid] = 0.f;
+                        Ek[q * bd + tid] = 0.f;
+                        Rk[q * bd + tid] = 0.f;
+                    }
                 }
             }
         }
         if (__all_sync(kFull, done)) break;
-        if ((iter & 1023u) == 0u) {
-            const bool late = global_ns() > t_end;
-            if (__any_sync(kFull, late)) {
-                if (lane == 0) atomicExch(&B.stats->error, UMCX_ERR_TIMEOUT);
-                break;
-            }
-        }
+        if (out_of_budget(B, iter, lane, t_end)) break;
 
-        // ---- one event: a voxel step (+ crossing), then a scatter when the free path is used up
         int dep_idx = -1;
         float dep_val = 0.f;
-        bool term = false;
+        Event ev;
+        ev.term = false;
         if (active) {
-            if (p.lx > 0.f) {
-                const unsigned mid = p.media & UMCX_LABEL_MASK;
-                const Medium m = sm[mid];
-                bool crossed;
-                int newvox = step<STRICT>(P, p, m, &crossed);
-                c_steps++;
-                if (++p.nsteps > P.step_cap) {
-                    term = true;
-                    c_cap++;
-                } else if (newvox != p.lastvox) {  // L285-310
-                    c_cross++;
-                    if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && mid > 0) ppath[(mid - 1) * blockDim.x + tid] += p.lz;
-                    if (P.issavevol) {
-                        const int gate = static_cast<int>(fminf(static_cast<float>(P.maxgate - 1),
-                                                                static_cast<float>(static_cast<int>(floorf((p.ly - P.tstart) * P.rtstep)))));
-                        if (gate >= 0) {
-                            dep_idx = p.lastvox + gate * static_cast<int>(P.dimxyz);
-                            dep_val = deposit_value<STRICT>(P, p, m);
-                        }
-                        p.lw = p.pw;
-                        p.lz = 0.f;
-                    }
-                    if (p.ly > P.tend) {
-                        term = true;
+            advance<false, REFLECT, true>(P, B.labels, sm, p, ev, c);
+            if (ev.crossed) {
+                const unsigned m = ev.left_mid;
+                if ((P.savedetflag & UMCX_DET_PPATH) && m > 0) ppath[(m - 1) * bd + tid] += ev.seg;
+                float F = 0.f, dF = 0.f;
+                if (P.issavevol && ev.gate >= 0) {
+                    dep_idx = ev.left_vox + ev.gate * static_cast<int>(P.dimxyz);
+                    dep_val = ev.dep_val;
+                    F = ev.dep_val;
+                    // derivative of this deposit with respect to its own label's mua along the fixed path
+                    if (P.outputtype == UMCX_OUT_ENERGY) {
+                        dF = ev.seg * p.pw;  // d(w0 (1 - e^-mua l))/dmua = l w1
                     } else {
-                        unsigned newmedia = (newvox >= 0) ? __ldg(B.labels + newvox) : 0u;
-                        const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
-                        if (REFLECT && m.a.w != n2) {
-                            c_refl++;
-                            if (reflect<STRICT>(p, m.a.w, n2)) {
-                                if (newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0) term = true;
-                            } else {
-                                newvox = p.lastvox;
-                                newmedia = p.media;
-                            }
-                        } else if (newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0)) {
-                            term = true;
+                        // fluence = integral of w over the segment; derivative -w0 (1 - (1 + x) e^-x) / mua^2,
+                        // x = mua l, by its series for small x (also the mua -> 0 limit -w0 l^2 / 2)
+                        const float mua = sm[m].a.x;
+                        const float x = mua * ev.seg;
+                        float i1;
+                        if (x < 0.1f) {
+                            i1 = ev.seg * ev.seg *
+                                 (0.5f + x * (-1.f / 3.f + x * (0.125f + x * (-1.f / 30.f + x * (1.f / 144.f)))));
+                        } else {
+                            i1 = (1.f - (1.f + x) * expf(-x)) / (mua * mua);
                         }
-                        if (!term) {
-                            p.lastvox = newvox;
-                            p.media = newmedia;
-                        }
+                        dF = -ev.w_before * i1;
                     }
                 }
+                S += F;
+                Lk[m * bd + tid] += ev.seg;
+                Qk[m * bd + tid] += ev.seg * S;
+                Tk[m * bd + tid] += F * ev.seg;
+                Ek[m * bd + tid] += dF;
             }
-            if (!term && p.lx <= 0.f) {
-                scatter<STRICT>(p, sm[p.media & UMCX_LABEL_MASK]);
-                c_scat++;
+            if (ev.scattered) {
+                Ck[ev.scat_mid * bd + tid] += 1.f;
+                Rk[ev.scat_mid * bd + tid] += S;
             }
         }
+        deposit_converged(B, false, nullptr, tid, lane, dep_idx, dep_val);
+        const bool tdet = ev.term && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
+        detect_converged(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
+            if (B.detp) write_detp(P, B, p, ppath + tid, bd, d, slot);
+            DetRecord r;
+            r.photon = cur;
+            r.det = d + 1;
+            r.weight = p.pw;
+            r.time = p.ly;
+            r.pad = 0.f;
+            B.detrec[slot] = r;
+            float* ext = B.detext + slot * static_cast<unsigned long long>(2 * K);
+            for (int q = 0; q < K; q++) {
+                ext[q] = Lk[q * bd + tid];
+                ext[K + q] = Ck[q * bd + tid];
+            }
+        });
+        if (ev.term) {
+            if ((p.media & UMCX_LABEL_MASK) != 0u) {
+                tot += p.launchw;
+                esc += p.pw;
+            }
+            for (int q = 0; q < K; q++) {
+                const float L = Lk[q * bd + tid];
+                const float lsq = L * S - Qk[q * bd + tid];
+                ga[q * bd + tid] += static_cast<double>(-lsq + Ek[q * bd + tid]);
+                const float mus = sm[q].a.y;
+                const float a = Ck[q * bd + tid] * S - Rk[q * bd + tid];
+                gs[q * bd + tid] += static_cast<double>((mus > 0.f ? a / mus : 0.f) - (lsq + Tk[q * bd + tid]));
+            }
+            active = false;
+        }
+    }
+    flush_tallies(B, lane, tot, esc, c);
+    // per-label gradient accumulators: warp reduction in FP64, one atomic per warp and label
+    for (int q = 0; q < K; q++) {
+        double a = ga[q * bd + tid], s = gs[q * bd + tid];
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_down_sync(kFull, a, off);
+            s += __shfl_down_sync(kFull, s, off);
+        }
+        if (lane == 0) {
+            atomicAdd(B.grad + q, a);
+            atomicAdd(B.grad + K + q, s);
+        }
+    }
+}
 
-        // ---- converged part: fluence deposit
-        if (P.aggregate) {
+// =============================================================================================== replay kernel
+// Regenerates each recorded detected photon from its index (its RNG seed) and accumulates -w_exit * l into the
+// voxel-wise mua Jacobian of its detector at every voxel it leaves (l = path inside that voxel).  The exit weight
+// and detector of the replayed photon are compared with the record; differences are counted.
+template <bool REFLECT>
+__global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers B) {
+    extern __shared__ float4 smem4[];
+    Medium* sm = reinterpret_cast<Medium*>(smem4);
+    load_media(P, B.media, sm);
+    const unsigned lane = lane_id();
+    PhotonFeed feed;
+    feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x, B.replay_count,
+              static_cast<unsigned long long>(gridDim.x) * blockDim.x);
+    const unsigned long long t_end = global_ns() + P.budget_ns;
+    Photon p;
+    p.media = 0;
+    p.lastvox = -1;
+    bool active = false, done = false;
+    Counters c;
+    DetRecord rec;
+    rec.det = 0;
+    rec.weight = 0.f;
+    unsigned mismatch = 0;
+    for (unsigned iter = 0;; iter++) {
+        if (!active && !done) {
+            unsigned long long k;
+            if (!feed.take(B.counter, &k, B.replay_count)) {
+                done = true;
+            } else {
+                rec = B.replay_list[k];
+                c.launch++;
+                active = start_photon<false>(P, B.labels, p, rec.photon);
+                if (!active) mismatch++;
+            }
+        }
+        if (__all_sync(kFull, done)) break;
+        if (out_of_budget(B, iter, lane, t_end)) break;
+        if (active) {
+            Event ev;
+            advance<false, REFLECT, true>(P, B.labels, sm, p, ev, c);
+            if (ev.crossed && ev.left_vox >= 0)
+                atomicAdd(B.jacobian + static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox,
+                          -rec.weight * ev.seg);
+            if (ev.term) {
+                const bool same = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend && det_hit(P.det[rec.det - 1], p) &&
+                                  p.pw == rec.weight;
+                if (!same) mismatch++;
+                active = false;
+            }
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) mismatch += __shfl_down_sync(kFull, mismatch, off);
+    if (lane == 0 && mismatch) atomicAdd(&B.stats->capped, static_cast<unsigned long long>(mismatch));
+    flush_tallies(B, lane, 0.0, 0.0, c);
+}
+
+// =============================================================================================== batched kernel
+// One simulation of a batch (192 bytes, staged in shared memory).  Member names match KParams so the engine
+// functions (launch, step, advance, ...) take either.
+struct SimDesc {
+    int nx, ny, nz, maxgate;
+    unsigned dimyz, dimxyz;
+    int isreflect, issavevol, outputtype, srctype;
+    unsigned step_cap, media_base;  // first Medium of this simulation in the batch's table
+    float tstart, tend, rtstep, unitinmm;
+    unsigned seeds[4];
+    unsigned long long label_off;      // byte offset of its labels in the label pool
+    unsigned long long out_off;        // element offset of its output volume in the output pool
+    unsigned long long photon_offset;  // photon index of its first photon (seeds photon i as in a single run)
+    unsigned long long nphoton;
+    float4 srcpos, srcdir, srcrdir, srcparam1, srcparam2;
+};
+static_assert(sizeof(SimDesc) == 192, "SimDesc layout");
+
+struct BParams {
+    const SimDesc* sims;              // [nsim]
+    const unsigned long long* begin;  // [nsim + 1]: prefix sums of photon counts (batch photon index space)
+    double* tallies;                  // [nsim][2]: escape, total (L765-770) per simulation
+    int nsim, total_media, aggregate, pad;
+    unsigned long long total;         // photons in the whole batch
+    unsigned long long budget_ns;
+};
+
+__device__ __forceinline__ void deposit_add64(const KBuffers& B, long long idx, float v) {
+    if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
+    else atomicAdd(B.fluence + idx, v);
+}
+
+// Many independent simulations (different grids, label counts, optics, sources and photon budgets) in one
+// persistent launch.  Lanes draw photon indices from one counter over the concatenated photon ranges; a binary
+// search over the prefix sums names the simulation, whose descriptor and optical table sit in shared memory.
+// Consecutive indices belong to the same simulation, so at any moment only one or two simulations are in flight and
+// their outputs stay in L2, while the tail of one simulation overlaps the start of the next.
+// Shared memory: SimDesc[nsim] | u64 begin[nsim + 1] (padded to 16 B) | Medium[total_media] | float aggbuf[blockDim]
+template <bool REFLECT>
+__global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers B) {
+    extern __shared__ float4 smem4[];
+    SimDesc* sd = reinterpret_cast<SimDesc*>(smem4);
+    unsigned long long* begin = reinterpret_cast<unsigned long long*>(sd + BP.nsim);
+    Medium* sm = reinterpret_cast<Medium*>(begin + ((BP.nsim + 2) & ~1));
+    float* aggbuf = reinterpret_cast<float*>(sm + BP.total_media);
+    {
+        const float4* s = reinterpret_cast<const float4*>(BP.sims);
+        float4* d = reinterpret_cast<float4*>(sd);
+        for (int k = threadIdx.x; k < BP.nsim * 12; k += blockDim.x) d[k] = s[k];
+        for (int k = threadIdx.x; k <= BP.nsim; k += blockDim.x) begin[k] = BP.begin[k];
+        const float4* ms = reinterpret_cast<const float4*>(B.media);
+        float4* md = reinterpret_cast<float4*>(sm);
+        for (int k = threadIdx.x; k < 3 * BP.total_media; k += blockDim.x) md[k] = ms[k];
+    }
+    __syncthreads();
+
+    const unsigned tid = threadIdx.x;
+    const unsigned lane = lane_id();
+    PhotonFeed feed;
+    feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + tid, BP.total,
+              static_cast<unsigned long long>(gridDim.x) * blockDim.x);
+    const unsigned long long t_end = global_ns() + BP.budget_ns;
+    Photon p;
+    p.media = 0;
+    p.lastvox = -1;
+    bool active = false, done = false;
+    int sim = 0, tally_sim = -1;
+    double tot = 0.0, esc = 0.0;
+    Counters c;
+
+    for (unsigned iter = 0;; iter++) {
+        if (!active && !done) {
+            unsigned long long g;
+            if (!feed.take(B.counter, &g, BP.total)) {
+                done = true;
+            } else {
+                int lo = 0, hi = BP.nsim - 1;  // largest s with begin[s] <= g
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (begin[mid] <= g) lo = mid;
+                    else hi = mid - 1;
+                }
+                sim = lo;
+                if (sim != tally_sim) {
+                    if (tally_sim >= 0 && (tot != 0.0 || esc != 0.0)) {
+                        atomicAdd(BP.tallies + 2 * tally_sim, esc);
+                        atomicAdd(BP.tallies + 2 * tally_sim + 1, tot);
+                    }
+                    tally_sim = sim;
+                    tot = 0.0;
+                    esc = 0.0;
+                }
+                const SimDesc& S = sd[sim];
+                c.launch++;
+                active = start_photon<false>(S, B.labels + S.label_off, p, S.photon_offset + (g - begin[sim]));
+            }
+        }
+        if (__all_sync(kFull, done)) break;
+        if (out_of_budget(B, iter, lane, t_end)) break;
+
+        long long dep_idx = -1;
+        float dep_val = 0.f;
+        Event ev;
+        ev.term = false;
+        if (active) {
+            const SimDesc& S = sd[sim];
+            advance<false, REFLECT, false>(S, B.labels + S.label_off, sm + S.media_base, p, ev, c);
+            if (ev.crossed && S.issavevol && ev.gate >= 0) {
+                dep_idx = static_cast<long long>(S.out_off) + ev.left_vox +
+                          static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz);
+                dep_val = ev.dep_val;
+            }
+        }
+        if (BP.aggregate) {
             const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
             if (__popc(hm) > 1) {
-                const unsigned grp = __match_any_sync(kFull, dep_idx >= 0 ? static_cast<unsigned>(dep_idx) : 0xFFFFFFFFu);
+                const unsigned grp = __match_any_sync(kFull, dep_idx >= 0 ? static_cast<unsigned long long>(dep_idx) : ~0ULL);
                 aggbuf[tid] = dep_val;
                 __syncwarp();
-                if (dep_idx >= 0) {
-                    const unsigned leader = __ffs(grp) - 1;
-                    if (lane == leader) {
-                        float s = 0.f;
-                        const unsigned base = tid & ~31u;
-                        for (unsigned g = grp; g; g &= g - 1) s += aggbuf[base + __ffs(g) - 1];
-                        deposit_add(B, dep_idx, s);
-                    }
+                if (dep_idx >= 0 && lane == __ffs(grp) - 1u) {
+                    float s = 0.f;
+                    const unsigned base = tid & ~31u;
+                    for (unsigned gm = grp; gm; gm &= gm - 1) s += aggbuf[base + __ffs(gm) - 1];
+                    deposit_add64(B, dep_idx, s);
                 }
                 __syncwarp();
             } else if (dep_idx >= 0) {
-                deposit_add(B, dep_idx, dep_val);
+                deposit_add64(B, dep_idx, dep_val);
             }
         } else if (dep_idx >= 0) {
-            deposit_add(B, dep_idx, dep_val);
+            deposit_add64(B, dep_idx, dep_val);
         }
-
-        // ---- termination: energy tallies (L765-770) and detection (L276-278, L429-435)
-        if (SAVEDET) {
-            const bool tdet = term && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
-            if (__any_sync(kFull, tdet)) {
-                for (int d = 0; d < P.detnum; d++) {
-                    const float4 dp = P.det[d];
-                    const bool hit = tdet && ((dp.x - p.px) * (dp.x - p.px) + (dp.y - p.py) * (dp.y - p.py) +
-                                                  (dp.z - p.pz) * (dp.z - p.pz) <
-                                              dp.w * dp.w);
-                    const unsigned hm = __ballot_sync(kFull, hit);
-                    if (hm == 0u) continue;
-                    const unsigned leader = __ffs(hm) - 1;
-                    unsigned long long base = 0;
-                    if (lane == leader) base = atomicAdd(&B.stats->detected, static_cast<unsigned long long>(__popc(hm)));
-                    base = __shfl_sync(kFull, base, leader);
-                    if (hit) {
-                        const unsigned long long slot = base + __popc(hm & ((1u << lane) - 1u));
-                        if (slot < P.maxdetphotons) {
-                            float* rec = B.detp + slot * static_cast<unsigned long long>(P.cols);
-                            int k = 0;
-                            if (P.savedetflag & UMCX_DET_ID) rec[k++] = static_cast<float>(d + 1);
-                            if (P.savedetflag & UMCX_DET_PPATH)
-                                for (int q = 0; q < P.ppathlen; q++) rec[k++] = ppath[q * blockDim.x + tid];
-                            if (P.savedetflag & UMCX_DET_EXITPOS) {
-                                rec[k++] = p.px;
-                                rec[k++] = p.py;
-                                rec[k++] = p.pz;
-                            }
-                            if (P.savedetflag & UMCX_DET_EXITDIR) {
-                                rec[k++] = p.vx;
-                                rec[k++] = p.vy;
-                                rec[k++] = p.vz;
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        if (term) {
+        if (ev.term) {
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
                 tot += p.launchw;
                 esc += p.pw;
@@ -657,29 +1144,18 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
             active = false;
         }
     }
-
-    // ---- per-warp reduction of the tallies, one set of atomics per warp
-    for (int off = 16; off > 0; off >>= 1) {
-        tot += __shfl_down_sync(kFull, tot, off);
-        esc += __shfl_down_sync(kFull, esc, off);
-        c_launch += __shfl_down_sync(kFull, c_launch, off);
-        c_steps += __shfl_down_sync(kFull, c_steps, off);
-        c_cross += __shfl_down_sync(kFull, c_cross, off);
-        c_scat += __shfl_down_sync(kFull, c_scat, off);
-        c_refl += __shfl_down_sync(kFull, c_refl, off);
-        c_cap += __shfl_down_sync(kFull, c_cap, off);
+    if (tally_sim >= 0 && (tot != 0.0 || esc != 0.0)) {
+        atomicAdd(BP.tallies + 2 * tally_sim, esc);
+        atomicAdd(BP.tallies + 2 * tally_sim + 1, tot);
     }
-    if (lane == 0) {
-        atomicAdd(&B.stats->total, tot);
-        atomicAdd(&B.stats->escape, esc);
-        atomicAdd(&B.stats->launched, static_cast<unsigned long long>(c_launch));
-        atomicAdd(&B.stats->steps, static_cast<unsigned long long>(c_steps));
-        atomicAdd(&B.stats->crossings, static_cast<unsigned long long>(c_cross));
-        atomicAdd(&B.stats->scatters, static_cast<unsigned long long>(c_scat));
-        atomicAdd(&B.stats->reflections, static_cast<unsigned long long>(c_refl));
-        if (c_cap) atomicAdd(&B.stats->capped, static_cast<unsigned long long>(c_cap));
-    }
+    flush_tallies(B, lane, 0.0, 0.0, c);
 }
+
+// detector readings and their per-label derivatives from the extended records (FP64 accumulation):
+//   R[d][t] += w,  dR/dmua_k[d][t] += -w L_k,  dR/dmus_k[d][t] += w (n_k / mus_k - L_k)
+__global__ void k_adjoint_reduce(const KParams P, const DetRecord* __restrict__ rec, const float* __restrict__ ext,
+                                 unsigned long long n, const Medium* __restrict__ media, double* __restrict__ read,
+                                 double* __restrict__ gmua, double* __restrict__ gmus);
 
 // rand01 known-answer dump (MCX_rand, L187-215)
 __global__ void k_rng_dump(unsigned s0, unsigned s1, unsigned s2, unsigned s3, unsigned long long offset,
