@@ -270,6 +270,12 @@ def run_gpu_arm(args) -> None:
     d_det = torch.empty(sim.maxdetphotons * 4, dtype=torch.float32, device=f"cuda:{device}")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
     stream = torch.cuda.current_stream()
+    tuning = {"block_size": args.block, "blocks_per_sm": args.blocks_per_sm, "aggregation": args.aggregation,
+              "source": "command line"}
+    if not (args.block or args.blocks_per_sm or args.aggregation) and not args.no_autotune:
+        # the project's autotuner: short timed runs (10 % of the photons) over block sizes and aggregation modes
+        tuning = dict(ctx.autotune(sim, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.1),
+                      source="autotune (10 % photon probes)")
 
     def barrier():
         if ws > 1:
@@ -354,7 +360,8 @@ def run_gpu_arm(args) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (generated configuration)",
             "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": int(args.photons), "grid": [60, 60, 60],
                        "gates": int(sim.dim[3]), "detectors": int(sim.detnum),
-                       "l2": "flushed between steps (256 MB write)", "parallelism": f"photon ranges x{ws}"},
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"photon ranges x{ws}",
+                       "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},
             "gpu_launches": args.steps,
@@ -402,8 +409,9 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--aggregation", type=int, default=0)
     ap.add_argument("--no-forms", action="store_true", help="skip the adjoint and batched forms")
+    ap.add_argument("--no-autotune", action="store_true", help="use the built-in launch defaults")
     ap.add_argument("--batch-sims", type=int, default=256)
-    ap.add_argument("--batch-scale", type=float, default=0.01,
+    ap.add_argument("--batch-scale", type=float, default=0.1,
                     help="photon-budget scale of the batched form (1.0 = the full 5.4e8-photon batch, ~4 min/run)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup

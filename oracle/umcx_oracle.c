@@ -60,6 +60,7 @@ typedef struct {
     f4 len;   /* remaining scattering length, time, path since last deposit, weight at last deposit */
     int16_t ix, iy, iz, flip;
     int lastvox, media;
+    unsigned nsteps, zsteps;  /* step count and consecutive zero-length steps (guards, see orc_sprint) */
 } orc_photon;
 
 typedef struct {
@@ -301,6 +302,12 @@ static int orc_sprint(const orc_ctx* c, orc_photon* p, orc_rng* r, float* ppath,
     while (p->len.x > 0.f) {
         int newvox = orc_step(c, p, c->media[p->media & UMCX_LABEL_MASK]);
         ev->steps++;
+        /* Guards absent from the reference (which would loop forever): a photon stops after 2^24 steps, or after
+         * 255 consecutive zero-length steps (a zero direction component at a grid face can bounce between a
+         * zero-length crossing and a reflection in place).  Terminating photons never reach either limit, so
+         * outputs are unchanged; the CUDA kernels apply the same rule. */
+        p->zsteps = (p->rvec.w == 0.f) ? p->zsteps + 1 : 0;
+        if (++p->nsteps > (1u << 24) || p->zsteps >= 255) return 1;
         if (newvox != p->lastvox) {
             ev->crossings++;
             if (s->issavedet && (s->savedetflag & UMCX_DET_PPATH) && ((p->media & UMCX_LABEL_MASK) > 0)) {

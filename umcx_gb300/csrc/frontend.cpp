@@ -11,6 +11,10 @@
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
+#include <atomic>
+#include <exception>
+#include <mutex>
+#include <thread>
 
 #if defined(UMCX_HAVE_ZLIB)
 #include <zlib.h>
@@ -532,16 +536,36 @@ void UserIO::initdomain() {
                 if (compile_shape(key, obj->front_member().second, &cs)) {
                     const bool layers = key.find("Layers") == 1;
                     const size_t nl = layers ? cs.layers.size() : 1;
-                    for (uint32_t z = 0; z < domain.nz; z++)
-                        for (uint32_t y = 0; y < domain.ny; y++)
-                            for (uint32_t x = 0; x < domain.nx; x++) {
-                                const int64_t idx = domain.index(static_cast<int>(x), static_cast<int>(y), static_cast<int>(z));
-                                const P3 p{x + 0.5f, y + 0.5f, z + 0.5f};
-                                for (size_t l = 0; l < nl; l++) {
-                                    const int label = eval_shape(cs, p, l);
-                                    if (label) domain.vol[static_cast<size_t>(idx)] = label;  // MCX_volume::mask, L138-140
-                                }
-                            }
+                    // z-slabs on host threads (every voxel is written by exactly one thread)
+                    std::atomic<uint32_t> nextz{0};
+                    std::exception_ptr err;
+                    std::mutex err_mutex;
+                    auto slabs = [&]() {
+                        try {
+                            for (uint32_t z; (z = nextz.fetch_add(1)) < domain.nz;)
+                                for (uint32_t y = 0; y < domain.ny; y++)
+                                    for (uint32_t x = 0; x < domain.nx; x++) {
+                                        const int64_t idx = domain.index(static_cast<int>(x), static_cast<int>(y), static_cast<int>(z));
+                                        const P3 p{x + 0.5f, y + 0.5f, z + 0.5f};
+                                        for (size_t l = 0; l < nl; l++) {
+                                            const int label = eval_shape(cs, p, l);
+                                            if (label) domain.vol[static_cast<size_t>(idx)] = label;  // MCX_volume::mask, L138-140
+                                        }
+                                    }
+                        } catch (...) {
+                            std::lock_guard<std::mutex> lock(err_mutex);
+                            if (!err) err = std::current_exception();
+                            nextz.store(domain.nz);
+                        }
+                    };
+                    const size_t nvox = static_cast<size_t>(domain.nx) * domain.ny * domain.nz;
+                    unsigned nthr = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+                    if (nvox < (1u << 16)) nthr = 1;
+                    std::vector<std::thread> pool;
+                    for (unsigned t = 1; t < nthr; t++) pool.emplace_back(slabs);
+                    slabs();
+                    for (auto& th : pool) th.join();
+                    if (err) std::rethrow_exception(err);
                 } else if (!(key == "Name" || key == "Grid" || key == "Origin")) {
                     throw std::runtime_error("shape construct" + key + " is not supported");
                 }

@@ -38,6 +38,8 @@ namespace umcx_dev {
 constexpr float kOneOverC0 = 3.335640951981520e-12f;  // L29
 constexpr float kPi = 3.1415926535897932385f;         // L30
 constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr unsigned kZeroStepLimit = 255;  // consecutive zero-length steps before a photon is stopped
+constexpr unsigned kDefaultStepCap = 1u << 24;  // steps of one photon before it is stopped
 
 enum Kind : int { kForward = 0, kAdjoint = 1, kReplay = 2 };
 
@@ -317,7 +319,7 @@ __device__ __forceinline__ bool skip_to_grid(const PV& P, Photon& p) {
 // MCX_photon::step, L315-338; returns the new voxel index (lastvox when the step ends inside the voxel).
 // *seg returns the distance moved.
 template <bool STRICT, class PV>
-__device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, bool* crossed) {
+__device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, bool* crossed, float* moved) {
     const float hx = fabsf((static_cast<float>(p.ix + (p.vx > 0.f)) - p.px) * p.rx);
     const float hy = fabsf((static_cast<float>(p.iy + (p.vy > 0.f)) - p.py) * p.ry);
     const float hz = fabsf((static_cast<float>(p.iz + (p.vz > 0.f)) - p.pz) * p.rz);
@@ -344,6 +346,7 @@ __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, boo
         p.ly += dist * m.b.w;
     }
     p.lz += dist;
+    *moved = dist;
     if (*crossed) {
         if (p.flip == 0) p.ix += (p.vx > 0.f ? 1 : -1);
         else if (p.flip == 1) p.iy += (p.vy > 0.f ? 1 : -1);
@@ -521,9 +524,16 @@ __device__ __forceinline__ void advance(const PV& P, const uint8_t* __restrict__
         const unsigned mid = p.media & UMCX_LABEL_MASK;
         const Medium m = sm[mid];
         bool crossed;
-        int newvox = step<STRICT>(P, p, m, &crossed);
+        float moved;
+        int newvox = step<STRICT>(P, p, m, &crossed, &moved);
         c.steps++;
-        if (++p.nsteps > P.step_cap) {
+        // zero-progress guard: a direction component that is exactly zero at a grid face can make a photon alternate
+        // forever between a zero-length crossing and a reflection that puts it back (the inverse direction is stale
+        // after a launch or a refraction, as in the reference); count consecutive zero-length steps in bits 16+ of
+        // `media` and stop the photon after kZeroStepLimit of them, like the step cap
+        if (moved == 0.f) p.media += 0x10000u;
+        else p.media &= 0xFFFFu;
+        if (++p.nsteps > P.step_cap || p.media >= (kZeroStepLimit << 16)) {
             ev.term = true;
             c.cap++;
         } else if (newvox != p.lastvox) {
