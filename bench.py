@@ -148,7 +148,7 @@ def run_reference_arm(args) -> None:
     import oracle
 
     try:
-        oracle.build(reference_root="/root/reference" if Path("/root/reference").exists() else None)
+        oracle.build(reference_root=None)  # rebuilds the reference program from its staged sources when needed
     except Exception:
         pass
     threads = os.cpu_count() or 1
