@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define UMCX_ABI_VERSION 1
+#define UMCX_ABI_VERSION 2
 
 /* status codes */
 enum {
@@ -106,7 +106,7 @@ typedef struct umcx_result {
     float kernel_ms;          /* device time of the propagation kernel (CUDA events) */
     float total_ms;           /* wall time of the whole call */
     int32_t status;           /* same as the return value */
-    int32_t reserved;
+    int32_t label_bits;       /* bits per voxel of the shared-memory label copy the kernel read (0: global memory) */
 } umcx_result;
 
 /* Launch tuning; zero fields mean "choose automatically" (autotuner cache or built-in default). */
@@ -116,6 +116,10 @@ typedef struct umcx_tuning {
     int32_t aggregation;      /* 0 auto, 1 plain atomics, 2 warp match-any aggregation of fluence adds */
     int32_t budget_ms;        /* wall-clock budget of one propagation launch; 0 = 300 000 ms.  When it runs out the
                                  kernel stops, the call returns UMCX_ERR_TIMEOUT and the context stays usable. */
+    int32_t label_pack;       /* 0 or 1: labels from global memory; 2: from a palette-packed copy in shared memory
+                                 whenever it fits (at most 16 distinct label bytes, 2 or 4 bits per voxel, 192 KB).
+                                 The results are the same either way. */
+    int32_t reserved;         /* 0 */
 } umcx_tuning;
 
 typedef struct umcx_context umcx_context;
@@ -214,8 +218,8 @@ void umcx_batch_destroy(umcx_batch* b);
 
 /*
  * Autotuner (no reference counterpart): times short runs (sim's photons scaled by `fraction`, at least 20 000) of
- * the forward kernel over block sizes, resident CTAs per SM and fluence-aggregation modes, keeps the fastest in
- * *best and installs it on ctx.  Device buffers as for umcx_gpu_forward_device.
+ * the forward kernel over block sizes and fluence-aggregation modes, keeps the fastest in *best and installs it on
+ * ctx.  Device buffers as for umcx_gpu_forward_device.
  */
 int umcx_autotune(umcx_context* ctx, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
                   const float* detpos, float* d_fluence, float* d_detp, double fraction, umcx_tuning* best,

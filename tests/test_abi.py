@@ -47,7 +47,7 @@ def test_struct_layouts():
 
     assert C.sizeof(Sim) == 168
     assert C.sizeof(Result) == 96
-    assert C.sizeof(Tuning) == 16
+    assert C.sizeof(Tuning) == 24
 
 
 def test_no_device_is_an_error_not_a_crash():

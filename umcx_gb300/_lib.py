@@ -69,7 +69,7 @@ class Result(C.Structure):
         ("kernel_ms", C.c_float),
         ("total_ms", C.c_float),
         ("status", C.c_int32),
-        ("reserved", C.c_int32),
+        ("label_bits", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -78,7 +78,7 @@ class Result(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("aggregation", C.c_int32),
-                ("budget_ms", C.c_int32)]
+                ("budget_ms", C.c_int32), ("label_pack", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Peaks(C.Structure):

@@ -189,8 +189,10 @@ class Context:
         return load().umcx_last_error(self._h).decode()
 
     def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0,
-                   budget_ms: int = 0) -> None:
-        t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms)
+                   budget_ms: int = 0, label_pack: int = 0) -> None:
+        """Launch tuning for later calls (0 = automatic).  label_pack: 1 reads labels from global memory, 2 from a
+        palette-packed copy in shared memory whenever it fits; results are identical either way."""
+        t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms, label_pack)
         check(load().umcx_set_tuning(self._h, C.byref(t)), self._h, "umcx_set_tuning")
 
     def forward(self, sim: Sim, labels, media, detpos=None) -> Forward:
@@ -282,7 +284,7 @@ class Context:
                                   C.byref(best), C.byref(ms))
         check(rc, self._h, "umcx_autotune")
         return {"block_size": best.block_size, "blocks_per_sm": best.blocks_per_sm, "aggregation": best.aggregation,
-                "probe_ms": ms.value}
+                "label_pack": best.label_pack, "probe_ms": ms.value}
 
     def rng_dump(self, seeds, photon_offset: int, nphoton: int, ndraw: int) -> np.ndarray:
         s = (C.c_uint32 * 4)(*[int(x) for x in seeds])

@@ -30,6 +30,7 @@ CU_UNITS = {
     "capi.cu": [],
     "kernels_fast.cu": [],
     "kernels_strict.cu": ["--fmad=false"],
+    "kernels_pack.cu": [],
     "kernels_adjoint.cu": [],
     "kernels_batch.cu": [],
     "peaks.cu": [],

@@ -51,6 +51,8 @@ struct umcx_context {
     std::string err;
     umcx_tuning tuning{};
     DevBuf labels, fluence, detp, media, stats, counter, scratch, accum64;
+    DevBuf packed, presence;  // palette-packed label copy and the 256-bit label-byte set it is planned from
+    int last_pack = 0;        // bits per voxel of the label copy the last forward launch read (0 = global labels)
     // adjoint state kept between umcx_gpu_forward_adjoint and umcx_gpu_backward
     DevBuf detrec, detext, grad, jac;
     umcx_sim adj_sim{};
@@ -174,6 +176,59 @@ KParams make_params(const umcx_sim* s, const float* detpos) {
 
 void set_device(umcx_context* ctx) { UMCX_CK(cudaSetDevice(ctx->device)); }
 
+// Palette-packed label copies are planned up to this size (the forward kernel holds one per CTA in shared memory).
+constexpr unsigned long long kMaxPackedBytes = 192ULL * 1024ULL;
+
+// Palette of the label bytes present (mask: 256-bit set) and the code of each: at most 16 distinct bytes, 2 bits
+// per voxel for up to 4 of them, else 4.  Fills P.palette / palette_bits / packed_words; false if it cannot pack.
+bool plan_palette(const unsigned mask[8], unsigned long long nvox, LabelCodes& codes, KParams& P) {
+    int distinct = 0;
+    unsigned bytes[16];
+    for (unsigned b = 0; b < 256u; b++) {
+        if (!((mask[b >> 5] >> (b & 31u)) & 1u)) continue;
+        if (distinct == 16) return false;
+        bytes[distinct++] = b;
+    }
+    if (distinct == 0) return false;
+    const int bits = distinct <= 4 ? 2 : 4;
+    const unsigned long long per = 32ULL / static_cast<unsigned>(bits);
+    unsigned long long words = (nvox + per - 1) / per;
+    words = (words + 3ULL) & ~3ULL;  // the kernel stages whole 16-byte vectors
+    if (words * sizeof(unsigned) > kMaxPackedBytes) return false;
+    std::memset(codes.c, 0, sizeof(codes.c));
+    std::memset(P.palette, 0, sizeof(P.palette));
+    for (int k = 0; k < distinct; k++) {
+        codes.c[bytes[k]] = static_cast<uint8_t>(k);
+        P.palette[k >> 2] |= bytes[k] << ((k & 3) * 8);
+    }
+    P.palette_bits = bits;
+    P.packed_words = static_cast<unsigned>(words);
+    return true;
+}
+
+// Build the palette-packed label copy for the fast forward kernel when the volume is small enough and has few label
+// bytes: one scan of the labels for the set of bytes present (read back to choose the palette), one packing pass.
+void prepare_packed_labels(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labels, KParams& P, KBuffers& B,
+                           cudaStream_t stream) {
+    if (ctx->tuning.label_pack != 2 || (s->flags & UMCX_SIM_STRICT_MATH)) return;
+    const unsigned long long nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
+    if (nvox > kMaxPackedBytes * 4ULL) return;  // does not fit even at 2 bits per voxel
+    UMCX_CK(ctx->presence.ensure(8 * sizeof(unsigned)));
+    UMCX_CK(cudaMemsetAsync(ctx->presence.ptr, 0, 8 * sizeof(unsigned), stream));
+    launch_label_presence(d_labels, nvox, static_cast<unsigned*>(ctx->presence.ptr), ctx->sm_count, stream);
+    UMCX_CK(cudaGetLastError());
+    unsigned mask[8];
+    UMCX_CK(cudaMemcpyAsync(mask, ctx->presence.ptr, sizeof(mask), cudaMemcpyDeviceToHost, stream));
+    UMCX_CK(cudaStreamSynchronize(stream));
+    LabelCodes codes;
+    if (!plan_palette(mask, nvox, codes, P)) return;
+    UMCX_CK(ctx->packed.ensure(P.packed_words * sizeof(unsigned)));
+    launch_label_pack(d_labels, nvox, P.palette_bits, codes, static_cast<unsigned*>(ctx->packed.ptr), P.packed_words,
+                      ctx->sm_count, stream);
+    UMCX_CK(cudaGetLastError());
+    B.packed = static_cast<const unsigned*>(ctx->packed.ptr);
+}
+
 // Enqueue one forward simulation on `stream`: clears the tallies and the output, launches the propagation kernel
 // between the context's two events.  All buffers are device buffers.
 void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labels, const float* media,
@@ -212,9 +267,11 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     B.stats = static_cast<KStats*>(ctx->stats.ptr);
     B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
     B.fluence64 = fp64 ? static_cast<double*>(ctx->accum64.ptr) : nullptr;
+    prepare_packed_labels(ctx, s, d_labels, P, B, stream);
 
     LaunchChoice lc = choose_launch(ctx->device, ctx->sm_count, ctx->tuning, s, P);
     P.aggregate = lc.aggregate;
+    ctx->last_pack = lc.pack;
     if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
     UMCX_CK(cudaEventRecord(ctx->ev0, stream));
     launch_forward(lc, P, B, stream, (s->flags & UMCX_SIM_STRICT_MATH) != 0);
@@ -246,6 +303,7 @@ void collect(umcx_context* ctx, const umcx_sim* s, cudaStream_t stream, umcx_res
         res->capped = st.capped;
         res->kernel_ms = ms;
         res->status = st.error ? UMCX_ERR_TIMEOUT : UMCX_OK;
+        res->label_bits = ctx->last_pack;
     }
     if (st.error) throw BudgetError("propagation kernel stopped at its wall-clock budget; results are partial");
 }
@@ -273,6 +331,7 @@ int umcx_create(umcx_context** out, int device) {
         UMCX_CK(cudaEventCreate(&ctx->ev1));
         UMCX_CK(configure_fast_kernels());
         UMCX_CK(configure_strict_kernels());
+        UMCX_CK(configure_packed_kernels());
         UMCX_CK(configure_adjoint_kernels());
         return UMCX_OK;
     });
@@ -296,6 +355,8 @@ void umcx_destroy(umcx_context* ctx) {
     ctx->counter.release();
     ctx->scratch.release();
     ctx->accum64.release();
+    ctx->packed.release();
+    ctx->presence.release();
     ctx->detrec.release();
     ctx->detext.release();
     ctx->grad.release();
@@ -472,6 +533,7 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         P.aggregate = 0;
         if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
         UMCX_CK(cudaEventRecord(ctx->ev0, st));
+        ctx->last_pack = 0;
         launch_adjoint(grid, block, smem, s->isreflect != 0, P, B, st);
         UMCX_CK(cudaGetLastError());
         UMCX_CK(cudaEventRecord(ctx->ev1, st));

@@ -1,10 +1,14 @@
 // kernels_fast.cu - instances of the production (fast-math) propagation kernels, the launch policy and the RNG
 // known-answer kernel.
 #include <algorithm>
+#include <cstdlib>
 
 #include "launch.h"
 
 namespace umcx_dev {
+
+// -1 leaves the driver's choice; 0 asks for the smallest shared-memory carve-out that fits the launch (largest L1)
+constexpr int kDefaultCarveout = -1;
 
 template <bool R, bool D>
 static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
@@ -31,7 +35,13 @@ static int occ_one(int block, size_t smem) {
 // allow the forward kernels up to 227 KB of dynamic shared memory (large per-thread partial-path scratch)
 template <bool R, bool D>
 static cudaError_t allow_big_smem() {
-    return cudaFuncSetAttribute(k_forward<false, R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(k_forward<false, R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    // prefer L1 over shared memory: the label volume is read through L1 at every voxel crossing
+    const char* pref = std::getenv("UMCX_SMEM_CARVEOUT");  // percent of the unified L1/shared array given to shared
+    const int carve = pref ? std::atoi(pref) : kDefaultCarveout;
+    if (e == cudaSuccess && carve >= 0)
+        e = cudaFuncSetAttribute(k_forward<false, R, D>, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+    return e;
 }
 cudaError_t configure_fast_kernels() {
     cudaError_t e = allow_big_smem<false, false>();
@@ -48,15 +58,17 @@ int occupancy_fast(bool reflect, bool savedet, int block, size_t smem) {
 
 void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st, bool strict) {
     if (strict) launch_forward_strict(lc, P, B, st);
+    else if (lc.pack) launch_forward_packed(lc, P, B, st);
     else launch_forward_fast(lc, P, B, st);
 }
 
-size_t forward_smem(const KParams& P, int block, bool savedet) {
+size_t forward_smem(const KParams& P, int block, bool savedet, int pack) {
     size_t s = 2 * sizeof(double) * static_cast<size_t>(block);  // per-lane energy tallies
     s += sizeof(Medium) * static_cast<size_t>(P.mediumnum);
     s += sizeof(float) * static_cast<size_t>(block);  // per-lane launch weight
     if (savedet) s += sizeof(float) * static_cast<size_t>(P.ppathlen) * static_cast<size_t>(block);
     s += sizeof(float) * static_cast<size_t>(block);  // aggregation buffer
+    if (pack) s += sizeof(unsigned) * static_cast<size_t>(P.packed_words);  // packed label copy
     return s;
 }
 
@@ -72,10 +84,23 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     const bool strict = (s->flags & UMCX_SIM_STRICT_MATH) != 0;
     lc.block = t.block_size > 0 ? t.block_size : 256;
     lc.aggregate = t.aggregation == 2 ? 1 : 0;
-    lc.smem = forward_smem(P, lc.block, lc.savedet);
+    lc.smem = forward_smem(P, lc.block, lc.savedet, 0);
     int occ = forward_occupancy(strict, lc.reflect, lc.savedet, lc.block, lc.smem);
     if (occ < 1) occ = 1;
-    const int per_sm = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
+    int per_sm = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
+    // shared-memory labels only on request: measured on GB300 they run at the speed of the global-memory reads
+    // (those hit L1) and cost resident CTAs when the copy is large
+    const int bits = P.palette_bits;
+    if (!strict && bits > 0 && P.packed_words > 0 && t.label_pack == 2) {
+        const size_t smem = forward_smem(P, lc.block, lc.savedet, bits);
+        int occ_p = smem <= 227u * 1024u ? occupancy_packed(lc.reflect, lc.savedet, bits, lc.block, smem) : 0;
+        const int per_sm_p = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ_p) : occ_p;
+        if (per_sm_p >= 1) {
+            lc.pack = bits;
+            lc.smem = smem;
+            per_sm = per_sm_p;
+        }
+    }
     lc.grid = sm_count * per_sm;
     // never launch more lanes than photons need (small runs): whole warps, at least one CTA
     const unsigned long long lanes = static_cast<unsigned long long>(lc.grid) * lc.block;

@@ -86,11 +86,15 @@ struct KParams {
     unsigned seeds[4];
     float4 srcpos, srcdir, srcrdir, srcparam1, srcparam2;
     unsigned long long budget_ns;  // wall-clock budget of the launch (checked against %globaltimer)
+    unsigned palette[4];           // palette-packed labels: label byte of each code (4 bytes per word)
+    unsigned packed_words;         // words of the packed label volume, a multiple of 4 (0 = not packed)
+    int palette_bits;              // bits per voxel of the packed volume (2 or 4; 0 = not packed)
     float4 det[UMCX_MAX_DET];
 };
 
 struct KBuffers {
     const uint8_t* labels;
+    const unsigned* packed;  // palette-packed labels (16-byte aligned, padded to whole uint4)
     float* fluence;
     double* fluence64;   // optional FP64 accumulation volume (same layout as fluence)
     float* detp;
@@ -493,15 +497,37 @@ struct Event {
     unsigned scat_mid;
 };
 
+// Label sources.  GlobalLabels reads the uint8 volume through the read-only path; PackedLabels reads a palette-
+// packed copy (BITS per voxel, 32/BITS voxels per 32-bit word) held in shared memory, with the palette (up to 16
+// label bytes) in registers.
+struct GlobalLabels {
+    const uint8_t* __restrict__ p;
+    __device__ __forceinline__ unsigned operator()(int i) const { return __ldg(p + i); }
+};
+
+template <int BITS>
+struct PackedLabels {
+    const unsigned* words;  // shared memory
+    uint4 pal;              // palette: byte k of the 16 is the label byte of code k
+    __device__ __forceinline__ unsigned operator()(int i) const {
+        constexpr int kPer = 32 / BITS;
+        constexpr int kShift = BITS == 2 ? 4 : 3;
+        const unsigned code = (words[i >> kShift] >> ((i & (kPer - 1)) * BITS)) & ((1u << BITS) - 1u);
+        if (BITS == 2) return (pal.x >> (code * 8u)) & 0xFFu;
+        const unsigned q = code >> 2;
+        const unsigned w = q == 0 ? pal.x : (q == 1 ? pal.y : (q == 2 ? pal.z : pal.w));
+        return (w >> ((code & 3u) * 8u)) & 0xFFu;
+    }
+};
+
 // L761-762 + L262-271: seed photon idx, launch it, move it onto the grid; false when it misses the grid
-template <bool STRICT, class PV>
-__device__ __forceinline__ bool start_photon(const PV& P, const uint8_t* __restrict__ labels, Photon& p,
-                                             unsigned long long idx) {
+template <bool STRICT, class PV, class LV>
+__device__ __forceinline__ bool start_photon(const PV& P, const LV& labels, Photon& p, unsigned long long idx) {
     p.launchw = launch<STRICT>(P, p, idx);
     p.lastvox = vox_index(P, p.ix, p.iy, p.iz);
     const bool inside = p.lastvox >= 0 || skip_to_grid(P, p);
     if (inside) {
-        p.media = __ldg(labels + p.lastvox);
+        p.media = labels(p.lastvox);
         p.lx = scat_len<STRICT>(p.rng);
     } else {
         p.media = 0;
@@ -514,9 +540,9 @@ __device__ __forceinline__ bool start_photon(const PV& P, const uint8_t* __restr
 // (L272-274).  Every kernel (forward, adjoint, replay) advances photons with this one function, so a replayed photon
 // follows the forward pass's trajectory.  RESET_SEGMENT resets the deposit segment at every crossing even when no
 // volume is saved (per-voxel path lengths for the adjoint and the replay); trajectories do not depend on it.
-template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV>
-__device__ __forceinline__ void advance(const PV& P, const uint8_t* __restrict__ labels, const Medium* sm,
-                                        Photon& p, Event& ev, Counters& c) {
+template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV, class LV>
+__device__ __forceinline__ void advance(const PV& P, const LV& labels, const Medium* sm, Photon& p, Event& ev,
+                                        Counters& c) {
     ev.crossed = false;
     ev.term = false;
     ev.scattered = false;
@@ -553,7 +579,7 @@ __device__ __forceinline__ void advance(const PV& P, const uint8_t* __restrict__
             if (p.ly > P.tend) {
                 ev.term = true;
             } else {
-                unsigned newmedia = (newvox >= 0) ? __ldg(labels + newvox) : 0u;
+                unsigned newmedia = (newvox >= 0) ? labels(newvox) : 0u;
                 const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
                 if (REFLECT && P.isreflect && m.a.w != n2) {
                     c.refl++;
@@ -716,7 +742,17 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
 
 // =============================================================================================== forward kernel
 // Shared memory: Medium[mediumnum] | float ppath[ppathlen][blockDim] | float aggbuf[blockDim]
-template <bool STRICT, bool REFLECT, bool SAVEDET>
+template <int PACK>
+struct LabelViewOf {
+    using type = PackedLabels<PACK>;
+};
+template <>
+struct LabelViewOf<0> {
+    using type = GlobalLabels;
+};
+
+// PACK = 0 reads labels from global memory; PACK = 2 or 4 reads the palette-packed copy staged in shared memory
+template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0>
 __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
@@ -726,6 +762,17 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
     float* ppath = reinterpret_cast<float*>(sm + P.mediumnum);
     float* aggbuf = ppath + (SAVEDET ? P.ppathlen * blockDim.x : 0);
     float* lwbuf = aggbuf + blockDim.x;
+    unsigned* lwords = reinterpret_cast<unsigned*>(lwbuf + blockDim.x);
+    typename LabelViewOf<PACK>::type labels;
+    if constexpr (PACK == 0) {
+        labels.p = B.labels;
+    } else {
+        const uint4* src = reinterpret_cast<const uint4*>(B.packed);
+        uint4* dst = reinterpret_cast<uint4*>(lwords);
+        for (unsigned k = threadIdx.x; k < (P.packed_words + 3u) / 4u; k += blockDim.x) dst[k] = src[k];
+        labels.words = lwords;
+        labels.pal = make_uint4(P.palette[0], P.palette[1], P.palette[2], P.palette[3]);
+    }
     load_media(P, B.media, sm);
 
     const unsigned tid = threadIdx.x;
@@ -749,7 +796,7 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
                 done = true;
             } else {
                 c.launch++;
-                active = start_photon<STRICT>(P, B.labels, p, P.photon_offset + k);
+                active = start_photon<STRICT>(P, labels, p, P.photon_offset + k);
                 lwbuf[tid] = p.launchw;
                 if (SAVEDET && active)
                     for (int q = 0; q < P.ppathlen; q++) ppath[q * blockDim.x + tid] = 0.f;
@@ -763,7 +810,7 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
         Event ev;
         ev.term = false;
         if (active) {
-            advance<STRICT, REFLECT, false>(P, B.labels, sm, p, ev, c);
+            advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c);
             if (ev.crossed) {
                 if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.left_mid > 0)
                     ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
@@ -849,7 +896,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             } else {
                 c.launch++;
                 cur = P.photon_offset + k;
-                active = start_photon<false>(P, B.labels, p, cur);
+                active = start_photon<false>(P, GlobalLabels{B.labels}, p, cur);
                 if (active) {
                     S = 0.f;
                     for (int q = 0; q < P.ppathlen; q++) ppath[q * bd + tid] = 0.f;
@@ -872,7 +919,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
         Event ev;
         ev.term = false;
         if (active) {
-            advance<false, REFLECT, true>(P, B.labels, sm, p, ev, c);
+            advance<false, REFLECT, true>(P, GlobalLabels{B.labels}, sm, p, ev, c);
             if (ev.crossed) {
                 const unsigned m = ev.left_mid;
                 if ((P.savedetflag & UMCX_DET_PPATH) && m > 0) ppath[(m - 1) * bd + tid] += ev.seg;
@@ -989,7 +1036,7 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
             } else {
                 rec = B.replay_list[k];
                 c.launch++;
-                active = start_photon<false>(P, B.labels, p, rec.photon);
+                active = start_photon<false>(P, GlobalLabels{B.labels}, p, rec.photon);
                 if (!active) mismatch++;
             }
         }
@@ -997,7 +1044,7 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
         if (out_of_budget(B, iter, lane, t_end)) break;
         if (active) {
             Event ev;
-            advance<false, REFLECT, true>(P, B.labels, sm, p, ev, c);
+            advance<false, REFLECT, true>(P, GlobalLabels{B.labels}, sm, p, ev, c);
             if (ev.crossed && ev.left_vox >= 0)
                 atomicAdd(B.jacobian + static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox,
                           -rec.weight * ev.seg);
@@ -1108,7 +1155,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 }
                 const SimDesc& S = sd[sim];
                 c.launch++;
-                active = start_photon<false>(S, B.labels + S.label_off, p, S.photon_offset + (g - begin[sim]));
+                active = start_photon<false>(S, GlobalLabels{B.labels + S.label_off}, p, S.photon_offset + (g - begin[sim]));
             }
         }
         if (__all_sync(kFull, done)) break;
@@ -1120,7 +1167,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         ev.term = false;
         if (active) {
             const SimDesc& S = sd[sim];
-            advance<false, REFLECT, false>(S, B.labels + S.label_off, sm + S.media_base, p, ev, c);
+            advance<false, REFLECT, false>(S, GlobalLabels{B.labels + S.label_off}, sm + S.media_base, p, ev, c);
             if (ev.crossed && S.issavevol && ev.gate >= 0) {
                 dep_idx = static_cast<long long>(S.out_off) + ev.left_vox +
                           static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz);
