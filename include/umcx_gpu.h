@@ -201,11 +201,15 @@ int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out);
  *
  * umcx_batch_create copies the host labels (uint8 [nx][ny][nz] each) and media tables, allocates the output pool and
  * captures the graph (memsets, one or more kernel launches -- simulations are split into launches only when their
- * descriptors and optical tables exceed a CTA's shared memory -- and the FP64-to-FP32 rounding).
+ * descriptors and optical tables exceed a CTA's shared memory -- and the FP64-to-FP32 rounding).  With labels NULL
+ * the batch's label pool starts zeroed and the caller writes each simulation's labels in place before the first run,
+ * at umcx_batch_labels(b, i) (for example with umcx_gpu_build_labels, no host copy at all).
  */
 typedef struct umcx_batch umcx_batch;
 int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const uint8_t* const* labels,
                       const float* const* media, umcx_batch** out);
+/* Device address of simulation i's uint8 label volume inside the batch's pool (NULL on a bad index). */
+uint8_t* umcx_batch_labels(umcx_batch* b, int i);
 /* Run the whole batch once (graph launch + synchronise).  total receives the summed tallies and event counts and
  * kernel_ms the device time of the graph. */
 int umcx_batch_run(umcx_batch* b, umcx_result* total);
@@ -224,6 +228,41 @@ void umcx_batch_destroy(umcx_batch* b);
 int umcx_autotune(umcx_context* ctx, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
                   const float* detpos, float* d_fluence, float* d_detp, double fraction, umcx_tuning* best,
                   float* best_ms);
+
+/*
+ * Device label builder (MCX_userio::initdomain, L537-604, and maskdetectors, L605-632, on the GPU; no reference
+ * counterpart as an entry point).  The domain is either a list of compiled shape constructs painted over a Grid fill
+ * value, or a host int32 volume (decoded JData input); detectors are then masked (bit 7) and the labels written as
+ * uint8 into d_labels (device, dim[0]*dim[1]*dim[2] bytes) -- the same bytes the host front end produces.  Every
+ * float comparison is evaluated with single roundings in the reference's order, so voxel-centre ties resolve as on
+ * the host.  Synchronous on ctx's stream.  A shape value the reference would read from a missing key gives
+ * UMCX_ERR_INPUT "type must be number, but is null"; a label without a medium gives UMCX_ERR_INPUT.
+ */
+enum { UMCX_SHAPE_SPHERE = 0, UMCX_SHAPE_BOX = 1, UMCX_SHAPE_XLAYER = 2, UMCX_SHAPE_YLAYER = 3, UMCX_SHAPE_ZLAYER = 4,
+       UMCX_SHAPE_CYLINDER = 5 };
+#define UMCX_SHAPE_HAS_TAG 0x1u   /* tag present (a shape that contains a voxel reads it) */
+#define UMCX_SHAPE_HAS_SIZE0 0x2u /* Box "Sip.ze" components present: 0x2, 0x4, 0x8 */
+#define UMCX_SHAPE_HAS_HI 0x10u   /* layer upper bound present */
+typedef struct umcx_shape_op {    /* one shape, or one layer of a layers construct (48 bytes) */
+    int32_t kind;                 /* UMCX_SHAPE_* */
+    int32_t tag;
+    uint32_t present;             /* UMCX_SHAPE_HAS_* bits */
+    float f[8];                   /* sphere: O[3], R; box: O[3], Sip.ze[3]; layer: lo, hi; cylinder: C0[3],
+                                     unit axis[3], squared axis length, R */
+    int32_t reserved;
+} umcx_shape_op;
+typedef struct umcx_domain {
+    uint32_t dim[3];
+    int32_t fill;                 /* Grid Tag: every voxel's label before the shapes */
+    const umcx_shape_op* ops;     /* shapes in input order (layers expanded in order) */
+    int32_t nops;
+    int32_t mediumnum;            /* labels must be < mediumnum */
+    const int32_t* volume;        /* host int32 volume [nx][ny][nz] used instead of fill + ops, or NULL */
+    const float* detpos;          /* [detnum][4] detector x, y, z, R (grid units) */
+    int32_t detnum;
+    int32_t reserved;
+} umcx_domain;
+int umcx_gpu_build_labels(umcx_context* ctx, const umcx_domain* dom, uint8_t* d_labels);
 
 /*
  * Debug known-answer hook for the random number generator (MCX_rand, L187-215): for photons

@@ -3,7 +3,7 @@
  *
  * A "job" is a parsed reference-style input: what the reference's MCX_userio (fangq/umcx src/umcx.cpp:451-721)
  * builds from a command line or JSON, turned into the flat arrays the GPU entry points of umcx_gpu.h take
- * (MCX_run_simulation's set-up, L786-810).  Callers that already hold a label volume and a media table call
+ * (MCX_run_simulation's set-up, L786-810).  umcx_job_build_labels is the one call here that uses the GPU.  Callers that already hold a label volume and a media table call
  * umcx_gpu_forward directly and never need a job.
  */
 #ifndef UMCX_HOST_H
@@ -28,6 +28,11 @@ enum { UMCX_ACTION_RUN = 0, UMCX_ACTION_DUMPJSON = 1, UMCX_ACTION_DUMPMASK = 2, 
 int umcx_job_from_args(umcx_job** job, int argc, const char* const argv[]);
 /* Parse a JSON input string as MCX_run_json does (L853-856). */
 int umcx_job_from_json(umcx_job** job, const char* json);
+/* umcx_job_from_args with flags.  UMCX_JOB_DEVICE_LABELS: shape constructs are compiled but not painted and
+ * detectors not masked on the host; umcx_job_labels returns NULL and the labels are made on the GPU by
+ * umcx_job_build_labels (a missing shape value is then reported there instead of here). */
+#define UMCX_JOB_DEVICE_LABELS 0x1u
+int umcx_job_from_args_ex(umcx_job** job, int argc, const char* const argv[], uint32_t flags);
 void umcx_job_free(umcx_job* job);
 const char* umcx_job_error(const umcx_job* job);
 int umcx_job_action(const umcx_job* job);
@@ -45,7 +50,13 @@ int umcx_job_isnormalized(const umcx_job* job);
 /* output normaliser for a total launched energy (L820) */
 float umcx_job_normalizer(const umcx_job* job, double energytotal);
 
-/* The rasterised domain with the reference's int32 encoding (sign bit = detector voxel), for --dumpmask parity. */
+/* Build the job's uint8 label volume on the GPU into d_labels (device, nx*ny*nz bytes) with
+ * umcx_gpu_build_labels: shapes painted over the Grid fill (or the decoded JData volume), detectors masked.  Gives
+ * the bytes of umcx_job_labels.  Works for jobs parsed with or without UMCX_JOB_DEVICE_LABELS. */
+int umcx_job_build_labels(const umcx_job* job, umcx_context* ctx, uint8_t* d_labels);
+
+/* The rasterised domain with the reference's int32 encoding (sign bit = detector voxel), for --dumpmask parity
+ * (UMCX_ERR_INPUT for a job parsed with UMCX_JOB_DEVICE_LABELS, whose domain exists only on the device). */
 int umcx_job_domain_dims(const umcx_job* job, uint32_t dims[3]);
 int umcx_job_domain_int32(const umcx_job* job, int32_t* out, size_t n);
 /* Write <ID>_vol.bnii like --dumpmask (L528-531) to `path`. */

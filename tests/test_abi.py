@@ -43,11 +43,13 @@ def test_python_signatures_cover_header():
 
 
 def test_struct_layouts():
-    from umcx_gb300._lib import Result, Sim, Tuning
+    from umcx_gb300._lib import Domain, Result, ShapeOp, Sim, Tuning
 
     assert C.sizeof(Sim) == 168
     assert C.sizeof(Result) == 96
     assert C.sizeof(Tuning) == 24
+    assert C.sizeof(ShapeOp) == 48
+    assert C.sizeof(Domain) == 56
 
 
 def test_no_device_is_an_error_not_a_crash():

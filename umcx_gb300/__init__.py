@@ -4,7 +4,7 @@ The compute path is libumcx_gb300.so (hand-written CUDA kernels + C ABI, include
 its Python binding and build script.
 """
 from ._lib import LIB_PATH, Result, Sim, Tuning, load
-from .api import Context, Forward, Job, detp_columns, measure_peaks, seeds_from_rngseed
+from .api import Batch, Context, Forward, Job, autotune_batch, detp_columns, measure_peaks, seeds_from_rngseed
 
-__all__ = ["LIB_PATH", "Result", "Sim", "Tuning", "load", "Context", "Forward", "Job", "detp_columns",
-           "measure_peaks", "seeds_from_rngseed"]
+__all__ = ["LIB_PATH", "Result", "Sim", "Tuning", "load", "Batch", "Context", "Forward", "Job", "autotune_batch",
+           "detp_columns", "measure_peaks", "seeds_from_rngseed"]

@@ -95,6 +95,23 @@ class Adjoint(C.Structure):
 
 assert C.sizeof(Sim) == 168, C.sizeof(Sim)
 
+class ShapeOp(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("tag", C.c_int32), ("present", C.c_uint32), ("f", C.c_float * 8),
+                ("reserved", C.c_int32)]
+
+
+class Domain(C.Structure):
+    _fields_ = [("dim", C.c_uint32 * 3), ("fill", C.c_int32), ("ops", C.POINTER(ShapeOp)), ("nops", C.c_int32),
+                ("mediumnum", C.c_int32), ("volume", C.c_void_p), ("detpos", C.c_void_p), ("detnum", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+assert C.sizeof(ShapeOp) == 48, C.sizeof(ShapeOp)
+
+UMCX_JOB_DEVICE_LABELS = 1
+SHAPE_SPHERE, SHAPE_BOX, SHAPE_XLAYER, SHAPE_YLAYER, SHAPE_ZLAYER, SHAPE_CYLINDER = range(6)
+SHAPE_HAS_TAG, SHAPE_HAS_SIZE0, SHAPE_HAS_HI = 0x1, 0x2, 0x10
+
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
 _U8P = C.POINTER(C.c_uint8)
@@ -118,6 +135,8 @@ SIGNATURES = [
     ("umcx_batch_get", C.c_int, [_P, C.c_int, _P, C.POINTER(Result)]),
     ("umcx_batch_set_tuning", C.c_int, [_P, C.POINTER(Tuning)]),
     ("umcx_batch_destroy", None, [_P]),
+    ("umcx_batch_labels", C.c_void_p, [_P, C.c_int]),
+    ("umcx_gpu_build_labels", C.c_int, [_P, C.POINTER(Domain), _P]),
     ("umcx_autotune", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, C.c_double, C.POINTER(Tuning),
                                 C.POINTER(C.c_float)]),
     ("umcx_gpu_rng_dump", C.c_int, [_P, C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32, C.c_uint32, _P]),
@@ -128,6 +147,8 @@ SIGNATURES = [
     ("umcx_main", C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
     ("umcx_job_from_args", C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(C.c_char_p)]),
     ("umcx_job_from_json", C.c_int, [C.POINTER(_P), C.c_char_p]),
+    ("umcx_job_from_args_ex", C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(C.c_char_p), C.c_uint32]),
+    ("umcx_job_build_labels", C.c_int, [_P, _P, _P]),
     ("umcx_job_free", None, [_P]),
     ("umcx_job_error", C.c_char_p, [_P]),
     ("umcx_job_action", C.c_int, [_P]),

@@ -33,10 +33,13 @@ class Job:
         self._h = handle
 
     @classmethod
-    def from_args(cls, args: list[str]) -> "Job":
+    def from_args(cls, args: list[str], device_labels: bool = False) -> "Job":
+        """Parse a reference command line.  device_labels=True leaves the shapes unpainted and the detectors
+        unmasked on the host: the label volume is then built on the GPU by build_labels (job.labels is None)."""
         lib = load()
         h = C.c_void_p()
-        rc = lib.umcx_job_from_args(C.byref(h), len(args) + 1, _argv(args))
+        flags = _lib.UMCX_JOB_DEVICE_LABELS if device_labels else 0
+        rc = lib.umcx_job_from_args_ex(C.byref(h), len(args) + 1, _argv(args), flags)
         job = cls(h)
         if rc != _lib.UMCX_OK:
             msg = lib.umcx_job_error(h).decode()
@@ -46,9 +49,9 @@ class Job:
         return job
 
     @classmethod
-    def from_json(cls, cfg) -> "Job":
+    def from_json(cls, cfg, device_labels: bool = False) -> "Job":
         text = cfg if isinstance(cfg, str) else json.dumps(cfg)
-        return cls.from_args(["--json", text])
+        return cls.from_args(["--json", text], device_labels)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -72,11 +75,20 @@ class Job:
         return load().umcx_job_sim(self._h).contents.copy()
 
     @property
-    def labels(self) -> np.ndarray:
+    def labels(self) -> np.ndarray | None:
+        """uint8 labels [nx, ny, nz] built on the host (None for a job parsed with device_labels=True)."""
         s = self.sim
         n = s.dim[0] * s.dim[1] * s.dim[2]
         p = load().umcx_job_labels(self._h)
+        if not p:
+            return None
         return np.ctypeslib.as_array(p, shape=(n,)).copy().reshape(s.dim[0], s.dim[1], s.dim[2])
+
+    def build_labels(self, ctx: "Context", d_labels) -> None:
+        """Build this job's uint8 label volume on the GPU (umcx_job_build_labels) into d_labels: a CUDA tensor of
+        nx*ny*nz bytes, or a device address (int)."""
+        ptr = d_labels if isinstance(d_labels, int) else d_labels.data_ptr()
+        check(load().umcx_job_build_labels(self._h, ctx.handle, C.c_void_p(ptr)), ctx.handle, "umcx_job_build_labels")
 
     @property
     def media(self) -> np.ndarray:
@@ -298,22 +310,36 @@ class Batch:
     """Many independent simulations in one persistent, graph-captured launch (umcx_batch_*)."""
 
     def __init__(self, ctx: Context, sims, labels, media):
+        """labels: one host uint8 volume per simulation, or None to write them in place afterwards (label_ptr)."""
         lib = load()
         n = len(sims)
         arr = (Sim * n)(*[s.copy() for s in sims])
-        self._keep = [np.ascontiguousarray(x, np.uint8) for x in labels] + [np.ascontiguousarray(m, np.float32)
-                                                                            for m in media]
-        lab = (C.c_void_p * n)(*[x.ctypes.data for x in self._keep[:n]])
-        med = (C.c_void_p * n)(*[m.ctypes.data for m in self._keep[n:]])
+        keep_lab = [] if labels is None else [np.ascontiguousarray(x, np.uint8) for x in labels]
+        keep_med = [np.ascontiguousarray(m, np.float32) for m in media]
+        lab = None if labels is None else (C.c_void_p * n)(*[x.ctypes.data for x in keep_lab])
+        med = (C.c_void_p * n)(*[m.ctypes.data for m in keep_med])
         self._ctx = ctx
         self._h = C.c_void_p()
         check(lib.umcx_batch_create(ctx.handle, n, arr, lab, med, C.byref(self._h)), ctx.handle, "umcx_batch_create")
         self.sims = [s.copy() for s in sims]
-        self._keep = None
 
     @classmethod
-    def from_jobs(cls, ctx: Context, jobs) -> "Batch":
-        return cls(ctx, [j.sim for j in jobs], [j.labels for j in jobs], [j.media for j in jobs])
+    def from_jobs(cls, ctx: Context, jobs, device_labels: bool = False) -> "Batch":
+        """Batch of parsed jobs.  device_labels=True builds every label volume on the GPU straight into the batch's
+        label pool (umcx_job_build_labels at umcx_batch_labels), with no host volume at all."""
+        if not device_labels:
+            return cls(ctx, [j.sim for j in jobs], [j.labels for j in jobs], [j.media for j in jobs])
+        b = cls(ctx, [j.sim for j in jobs], None, [j.media for j in jobs])
+        for i, j in enumerate(jobs):
+            j.build_labels(ctx, b.label_ptr(i))
+        return b
+
+    def label_ptr(self, i: int) -> int:
+        """Device address of simulation i's uint8 labels in the batch's pool (umcx_batch_labels)."""
+        p = load().umcx_batch_labels(self._h, int(i))
+        if not p:
+            raise IndexError(i)
+        return int(p)
 
     def run(self) -> Result:
         r = Result()

@@ -35,6 +35,7 @@ CU_UNITS = {
     "kernels_batch.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],
+    "raster.cu": [],
 }
 CPP_UNITS = ["jsonlite.cpp", "frontend.cpp", "run.cpp"]
 

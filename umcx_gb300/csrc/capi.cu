@@ -52,6 +52,7 @@ struct umcx_context {
     umcx_tuning tuning{};
     DevBuf labels, fluence, detp, media, stats, counter, scratch, accum64;
     DevBuf packed, presence;  // palette-packed label copy and the 256-bit label-byte set it is planned from
+    DevBuf raster, raster_ops, raster_coords;  // device label builder: int32 volume + marks + flags, ops, lattices
     int last_pack = 0;        // bits per voxel of the label copy the last forward launch read (0 = global labels)
     // adjoint state kept between umcx_gpu_forward_adjoint and umcx_gpu_backward
     DevBuf detrec, detext, grad, jac;
@@ -357,6 +358,9 @@ void umcx_destroy(umcx_context* ctx) {
     ctx->accum64.release();
     ctx->packed.release();
     ctx->presence.release();
+    ctx->raster.release();
+    ctx->raster_ops.release();
+    ctx->raster_coords.release();
     ctx->detrec.release();
     ctx->detext.release();
     ctx->grad.release();
@@ -631,6 +635,93 @@ int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out) {
     });
 }
 
+int umcx_gpu_build_labels(umcx_context* ctx, const umcx_domain* dom, uint8_t* d_labels) {
+    if (!ctx) return UMCX_ERR_INPUT;
+    return guarded(ctx, [&]() {
+        if (!dom || !d_labels) throw InputError("domain or labels is NULL");
+        for (int k = 0; k < 3; k++)
+            if (dom->dim[k] < 1 || dom->dim[k] > 32767) throw InputError("domain dimensions must be between 1 and 32767");
+        if (dom->nops < 0 || (dom->nops > 0 && !dom->ops)) throw InputError("shape ops missing");
+        if (dom->mediumnum < 1 || dom->mediumnum > UMCX_MAX_MEDIA) throw InputError("mediumnum must be in [1, 128]");
+        if (dom->detnum < 0 || dom->detnum > UMCX_MAX_DET || (dom->detnum > 0 && !dom->detpos))
+            throw InputError("detnum must be in [0, 64] with detpos given");
+        set_device(ctx);
+        cudaStream_t st = ctx->stream;
+        const unsigned long long n = 1ULL * dom->dim[0] * dom->dim[1] * dom->dim[2];
+        // working buffer: int32 volume | marks (n bytes, rounded to 256) | flags: missing (u32), first bad index (u64)
+        const size_t vbytes = n * sizeof(int32_t), mbytes = (n + 255) & ~255ULL;
+        UMCX_CK(ctx->raster.ensure(vbytes + mbytes + 256));
+        int32_t* vol = static_cast<int32_t*>(ctx->raster.ptr);
+        uint8_t* mark = reinterpret_cast<uint8_t*>(vol) + vbytes;
+        unsigned* missing = reinterpret_cast<unsigned*>(mark + mbytes);
+        unsigned long long* first_bad = reinterpret_cast<unsigned long long*>(mark + mbytes + 8);
+        const unsigned long long none = ~0ULL;
+        UMCX_CK(cudaMemsetAsync(mark, 0, mbytes + 8, st));
+        UMCX_CK(cudaMemcpyAsync(first_bad, &none, sizeof(none), cudaMemcpyHostToDevice, st));
+        if (dom->volume) {
+            UMCX_CK(cudaMemcpyAsync(vol, dom->volume, vbytes, cudaMemcpyHostToDevice, st));
+        } else {
+            if (dom->nops > 0) {
+                UMCX_CK(ctx->raster_ops.ensure(sizeof(umcx_shape_op) * static_cast<size_t>(dom->nops)));
+                UMCX_CK(cudaMemcpyAsync(ctx->raster_ops.ptr, dom->ops, sizeof(umcx_shape_op) * static_cast<size_t>(dom->nops),
+                                        cudaMemcpyHostToDevice, st));
+            }
+            launch_raster(static_cast<const umcx_shape_op*>(ctx->raster_ops.ptr), dom->nops, dom->fill, dom->dim, vol,
+                          missing, ctx->sm_count, st);
+            UMCX_CK(cudaGetLastError());
+        }
+        // detector lattices (L607-609): the coordinates come from the reference's own float accumulation
+        // (start = -R - 1 + centre, step 0.5, while <= R + 1 + centre), generated here in the same order
+        std::vector<float> coords;
+        std::vector<DetLattice> lat(static_cast<size_t>(dom->detnum));
+        constexpr size_t kMaxSamplesPerAxis = 1u << 16;
+        for (int d = 0; d < dom->detnum; d++) {
+            const float* dp = dom->detpos + 4 * d;
+            DetLattice& L = lat[static_cast<size_t>(d)];
+            L.x = dp[0];
+            L.y = dp[1];
+            L.z = dp[2];
+            L.r = dp[3];
+            unsigned* offs[3] = {&L.xoff, &L.yoff, &L.zoff};
+            unsigned* cnts[3] = {&L.nxs, &L.nys, &L.nzs};
+            for (int a = 0; a < 3; a++) {
+                const float radius = dp[3], c = dp[a];
+                *offs[a] = static_cast<unsigned>(coords.size());
+                size_t cnt = 0;
+                for (float v = -radius - 1.f + c; v <= radius + 1.f + c; v += 0.5f) {
+                    if (++cnt > kMaxSamplesPerAxis) throw InputError("detector radius too large to mask");
+                    coords.push_back(v);
+                }
+                *cnts[a] = static_cast<unsigned>(cnt);
+            }
+        }
+        if (!coords.empty()) {
+            UMCX_CK(ctx->raster_coords.ensure(coords.size() * sizeof(float)));
+            UMCX_CK(cudaMemcpyAsync(ctx->raster_coords.ptr, coords.data(), coords.size() * sizeof(float),
+                                    cudaMemcpyHostToDevice, st));
+            for (const DetLattice& L : lat) {
+                launch_mask_det(vol, dom->dim, L, static_cast<const float*>(ctx->raster_coords.ptr), mark, ctx->sm_count,
+                                st);
+                UMCX_CK(cudaGetLastError());
+            }
+        }
+        launch_finish_labels(vol, mark, n, dom->mediumnum, d_labels, first_bad, ctx->sm_count, st);
+        UMCX_CK(cudaGetLastError());
+        unsigned flags_miss = 0;
+        unsigned long long bad = none;
+        UMCX_CK(cudaMemcpyAsync(&flags_miss, missing, sizeof(flags_miss), cudaMemcpyDeviceToHost, st));
+        UMCX_CK(cudaMemcpyAsync(&bad, first_bad, sizeof(bad), cudaMemcpyDeviceToHost, st));
+        UMCX_CK(cudaStreamSynchronize(st));  // the host vectors above stay alive until the copies are done
+        if (flags_miss) throw InputError("type must be number, but is null");
+        if (bad != none) {
+            int32_t v = 0;
+            UMCX_CK(cudaMemcpy(&v, vol + bad, sizeof(v), cudaMemcpyDeviceToHost));
+            throw InputError("label " + std::to_string(v & 0x7FFFFFFF) + " has no entry in Domain.Media");
+        }
+        return UMCX_OK;
+    });
+}
+
 int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photon_offset, uint32_t nphoton,
                       uint32_t ndraw, float* out) {
     if (!ctx) return UMCX_ERR_INPUT;
@@ -700,7 +791,7 @@ struct umcx_batch {
     umcx_context* ctx = nullptr;
     int nsim = 0;
     std::vector<umcx_sim> sims;
-    std::vector<unsigned long long> out_off;
+    std::vector<unsigned long long> out_off, label_off;
     unsigned long long nout_total = 0;
     bool reflect = false, fp64 = true;
     struct Chunk {
@@ -862,7 +953,7 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
     if (!b) return UMCX_ERR_INPUT;
     b->ctx = ctx;
     int rc = guarded(ctx, [&]() {
-        if (nsim < 1 || !sims || !labels || !media) throw InputError("empty batch or NULL arrays");
+        if (nsim < 1 || !sims || !media) throw InputError("empty batch or NULL arrays");
         set_device(ctx);
         UMCX_CK(configure_batch_kernels());
         b->nsim = nsim;
@@ -877,7 +968,8 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
             validate(s);
             if (s->issavedet) throw InputError("simulation " + std::to_string(i) + ": batches do not save detected photons");
             if (s->flags & UMCX_SIM_STRICT_MATH) throw InputError("batches run the fast-math kernel only");
-            if (!labels[i] || !media[i]) throw InputError("simulation " + std::to_string(i) + ": NULL labels or media");
+            if ((labels && !labels[i]) || !media[i])
+                throw InputError("simulation " + std::to_string(i) + ": NULL labels or media");
             const unsigned long long nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
             label_off[static_cast<size_t>(i)] = lab_total;
             lab_total += (nvox + 15) & ~15ULL;
@@ -924,7 +1016,9 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
         for (size_t c = 0; c < b->chunks.size(); c++) b->chunks[c].photons = totals[c];
         // device buffers
         UMCX_CK(b->labels.ensure(lab_total));
-        for (int i = 0; i < nsim; i++) {
+        b->label_off = label_off;
+        if (!labels) UMCX_CK(cudaMemset(b->labels.ptr, 0, lab_total));  // filled in place by the caller
+        for (int i = 0; labels && i < nsim; i++) {
             const unsigned long long nvox = 1ULL * sims[i].dim[0] * sims[i].dim[1] * sims[i].dim[2];
             UMCX_CK(cudaMemcpy(static_cast<uint8_t*>(b->labels.ptr) + label_off[static_cast<size_t>(i)], labels[i], nvox,
                                cudaMemcpyHostToDevice));
@@ -1025,6 +1119,11 @@ int umcx_batch_set_tuning(umcx_batch* b, const umcx_tuning* t) {
         batch_capture(b);
         return UMCX_OK;
     });
+}
+
+uint8_t* umcx_batch_labels(umcx_batch* b, int i) {
+    if (!b || i < 0 || i >= b->nsim || !b->labels.ptr) return nullptr;
+    return static_cast<uint8_t*>(b->labels.ptr) + b->label_off[static_cast<size_t>(i)];
 }
 
 void umcx_batch_destroy(umcx_batch* b) {

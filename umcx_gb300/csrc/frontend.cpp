@@ -5,6 +5,8 @@
 // on the same input (tests/test_frontend.py compares them with the reference's own --dumpmask output).
 #include "frontend.h"
 
+#include "shape_eval.h"
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -102,7 +104,7 @@ std::string UserIO::help_text() const {
     return s;
 }
 
-UserIO::UserIO(int argc, const char* const argv[]) {
+UserIO::UserIO(int argc, const char* const argv[], bool device_domain) : domain_on_device(device_domain) {
     if (argc < 0) throw std::runtime_error("binary JSON buffer input (MATLAB MEX path) is not supported");
     if (argc <= 1) {  // L480
         action = Action::Help;
@@ -337,111 +339,76 @@ static float need(const OptF& f) {
     return f.v;
 }
 
-struct CompiledShape {
-    enum Kind { kSphere, kBox, kXLayers, kYLayers, kZLayers, kCylinder } kind = kSphere;
-    float o[3] = {0, 0, 0}, r = 0;                     // sphere / box origin, radius
-    OptF boxsize[3];                                   // Box: the "Sip.ze" key the reference reads
-    float ax = 0, ay = 0, az = 0, d0 = 0, vx = 0, vy = 0, vz = 0, c0[3] = {0, 0, 0};  // cylinder
-    int tag = 0;
-    bool tag_ok = false;
-    struct Layer {
-        OptF lo, hi;
-        int tag = 0;
-        bool tag_ok = false;
-    };
-    std::vector<Layer> layers;
-};
-
-static bool compile_shape(const std::string& key, const Value& body, CompiledShape* cs) {
-    auto read_tag = [&](const Value& v, int* tag, bool* ok) {
+// Compiles one shape construct into device-evaluable ops (shape_eval.h), appended to *ops: a layers construct
+// gives one op per layer, in order.  Values every voxel reads are required here (the reference throws at the first
+// voxel); values read only inside a shape (the tag, the Box extent, a layer's upper bound) are recorded as present
+// or not and reported where a voxel reaches them.  Returns false for a key that is not a shape.
+static bool compile_shape(const std::string& key, const Value& body, std::vector<umcx_shape_op>* ops) {
+    auto read_tag = [&](const Value& v, umcx_shape_op* op) {
         const Value* t = v.find("Tag");
-        *ok = t && (t->is_number() || t->is_bool());
-        *tag = *ok ? t->as_int() : 0;
+        if (t && (t->is_number() || t->is_bool())) {
+            op->tag = t->as_int();
+            op->present |= UMCX_SHAPE_HAS_TAG;
+        }
     };
+    umcx_shape_op op;
+    std::memset(&op, 0, sizeof(op));
     if (key == "Sphere") {
-        cs->kind = CompiledShape::kSphere;
-        for (int k = 0; k < 3; k++) cs->o[k] = need(opt_num(body, "O", static_cast<size_t>(k)));
-        cs->r = need(opt_scalar(body.contains("R") ? body.at("R") : Value()));
-        read_tag(body, &cs->tag, &cs->tag_ok);
+        op.kind = UMCX_SHAPE_SPHERE;
+        for (int k = 0; k < 3; k++) op.f[k] = need(opt_num(body, "O", static_cast<size_t>(k)));
+        op.f[3] = need(opt_scalar(body.contains("R") ? body.at("R") : Value()));
+        read_tag(body, &op);
+        ops->push_back(op);
     } else if (key == "Box") {
         // the reference reads a key spelled "Sip.ze" and compares p.x three times (L460)
-        cs->kind = CompiledShape::kBox;
-        for (int k = 0; k < 3; k++) cs->o[k] = need(opt_num(body, "O", static_cast<size_t>(k)));
-        for (int k = 0; k < 3; k++) cs->boxsize[k] = opt_num(body, "Sip.ze", static_cast<size_t>(k));
-        read_tag(body, &cs->tag, &cs->tag_ok);
+        op.kind = UMCX_SHAPE_BOX;
+        for (int k = 0; k < 3; k++) op.f[k] = need(opt_num(body, "O", static_cast<size_t>(k)));
+        for (int k = 0; k < 3; k++) {
+            const OptF sz = opt_num(body, "Sip.ze", static_cast<size_t>(k));
+            op.f[3 + k] = sz.v;
+            if (sz.ok) op.present |= UMCX_SHAPE_HAS_SIZE0 << k;
+        }
+        read_tag(body, &op);
+        ops->push_back(op);
     } else if (key == "XLayers" || key == "YLayers" || key == "ZLayers") {
-        cs->kind = key[0] == 'X' ? CompiledShape::kXLayers : (key[0] == 'Y' ? CompiledShape::kYLayers : CompiledShape::kZLayers);
+        const int kind = key[0] == 'X' ? UMCX_SHAPE_XLAYER : (key[0] == 'Y' ? UMCX_SHAPE_YLAYER : UMCX_SHAPE_ZLAYER);
         for (const Value& layer : body.items()) {
-            CompiledShape::Layer L;
+            umcx_shape_op L;
+            std::memset(&L, 0, sizeof(L));
+            L.kind = kind;
             if (!layer.is_array()) missing_number();
-            L.lo = layer.size() > 0 ? opt_scalar(layer.at(0)) : OptF();
-            L.hi = layer.size() > 1 ? opt_scalar(layer.at(1)) : OptF();
+            const OptF lo = layer.size() > 0 ? opt_scalar(layer.at(0)) : OptF();
+            const OptF hi = layer.size() > 1 ? opt_scalar(layer.at(1)) : OptF();
+            L.f[0] = need(lo);
+            L.f[1] = hi.v;
+            if (hi.ok) L.present |= UMCX_SHAPE_HAS_HI;
             if (layer.size() > 2 && (layer.at(2).is_number() || layer.at(2).is_bool())) {
                 L.tag = layer.at(2).as_int();
-                L.tag_ok = true;
+                L.present |= UMCX_SHAPE_HAS_TAG;
             }
-            need(L.lo);
-            cs->layers.push_back(L);
+            ops->push_back(L);
         }
     } else if (key == "Cylinder") {
-        cs->kind = CompiledShape::kCylinder;
-        float c1[3];
+        op.kind = UMCX_SHAPE_CYLINDER;
+        float c0[3], c1[3];
         for (int k = 0; k < 3; k++) {
-            cs->c0[k] = need(opt_num(body, "C0", static_cast<size_t>(k)));
+            c0[k] = need(opt_num(body, "C0", static_cast<size_t>(k)));
             c1[k] = need(opt_num(body, "C1", static_cast<size_t>(k)));
         }
-        cs->ax = c1[0] - cs->c0[0];
-        cs->ay = c1[1] - cs->c0[1];
-        cs->az = c1[2] - cs->c0[2];
-        cs->d0 = cs->ax * cs->ax + cs->ay * cs->ay + cs->az * cs->az;
-        cs->vx = cs->ax / sqrtf(cs->d0);
-        cs->vy = cs->ay / sqrtf(cs->d0);
-        cs->vz = cs->az / sqrtf(cs->d0);
-        cs->r = need(opt_scalar(body.contains("R") ? body.at("R") : Value()));
-        read_tag(body, &cs->tag, &cs->tag_ok);
+        const float ax = c1[0] - c0[0], ay = c1[1] - c0[1], az = c1[2] - c0[2];
+        const float d0 = ax * ax + ay * ay + az * az;
+        for (int k = 0; k < 3; k++) op.f[k] = c0[k];
+        op.f[3] = ax / sqrtf(d0);
+        op.f[4] = ay / sqrtf(d0);
+        op.f[5] = az / sqrtf(d0);
+        op.f[6] = d0;
+        op.f[7] = need(opt_scalar(body.contains("R") ? body.at("R") : Value()));
+        read_tag(body, &op);
+        ops->push_back(op);
     } else {
         return false;
     }
     return true;
-}
-
-static int inside_tag(int tag, bool ok) {
-    if (!ok) missing_number();
-    return tag;
-}
-
-// label painted by one shape at voxel centre p (0 = none)
-static int eval_shape(const CompiledShape& cs, const P3& p, size_t layer) {
-    switch (cs.kind) {
-        case CompiledShape::kSphere:
-            return ((p.x - cs.o[0]) * (p.x - cs.o[0]) + (p.y - cs.o[1]) * (p.y - cs.o[1]) +
-                        (p.z - cs.o[2]) * (p.z - cs.o[2]) <
-                    (cs.r * cs.r))
-                       ? inside_tag(cs.tag, cs.tag_ok)
-                       : 0;
-        case CompiledShape::kBox: {
-            if (p.x < cs.o[0] || p.y < cs.o[1] || p.z < cs.o[2]) return 0;
-            const bool outside = p.x > cs.o[0] + need(cs.boxsize[0]) || p.x > cs.o[1] + need(cs.boxsize[1]) ||
-                                 p.x > cs.o[2] + need(cs.boxsize[2]);
-            return !outside ? inside_tag(cs.tag, cs.tag_ok) : 0;
-        }
-        case CompiledShape::kXLayers:
-        case CompiledShape::kYLayers:
-        case CompiledShape::kZLayers: {
-            const CompiledShape::Layer& L = cs.layers[layer];
-            const float c = cs.kind == CompiledShape::kXLayers ? p.x : (cs.kind == CompiledShape::kYLayers ? p.y : p.z);
-            return (c >= L.lo.v && c <= need(L.hi)) ? inside_tag(L.tag, L.tag_ok) : 0;
-        }
-        case CompiledShape::kCylinder: {
-            const float px = p.x - cs.c0[0], py = p.y - cs.c0[1], pz = p.z - cs.c0[2];
-            const float d = cs.vx * px + cs.vy * py + cs.vz * pz;
-            // the axial bound compares the projection with the SQUARED axis length (L469)
-            return (d <= cs.d0 && d >= 0.f && px * px + py * py + pz * pz - d * d <= cs.r * cs.r)
-                       ? inside_tag(cs.tag, cs.tag_ok)
-                       : 0;
-        }
-    }
-    return 0;
 }
 
 std::vector<unsigned char> base64_decode(const std::string& in) {
@@ -513,17 +480,90 @@ static void copy_cast(const std::vector<unsigned char>& raw, std::vector<int32_t
 
 void UserIO::initdomain() {
     const Value& dim = cfg.at("Domain").at("Dim");
-    domain.reshape(static_cast<uint32_t>(dim.at(0).as_uint64()), static_cast<uint32_t>(dim.at(1).as_uint64()),
-                   static_cast<uint32_t>(dim.at(2).as_uint64()));
+    uint32_t nx = static_cast<uint32_t>(dim.at(0).as_uint64()), ny = static_cast<uint32_t>(dim.at(1).as_uint64()),
+             nz = static_cast<uint32_t>(dim.at(2).as_uint64());
+    shape_ops.clear();
+    grid_fill = 0;
+    domain_is_volume = false;
     const Value* shapes = cfg.find("Shapes");
-    if (shapes) {
-        if (!shapes->contains("_ArraySize_")) {
-            const Value& first = shapes->is_array() ? shapes->at(0) : *shapes;
-            if (const Value* grid = first.find("Grid")) {
-                const Value& sz = grid->at("Size");
-                domain.reshape(static_cast<uint32_t>(sz.at(0).as_uint64()), static_cast<uint32_t>(sz.at(1).as_uint64()),
-                               static_cast<uint32_t>(sz.at(2).as_uint64()), grid->at("Tag").as_int());
+    if (shapes && shapes->contains("_ArraySize_")) {  // JData volume (L571-598): decoded on the host
+        domain_is_volume = true;
+        const Value& sz = shapes->at("_ArraySize_");
+        domain.reshape(static_cast<uint32_t>(sz.at(0).as_uint64()), static_cast<uint32_t>(sz.at(1).as_uint64()),
+                       static_cast<uint32_t>(sz.at(2).as_uint64()));
+        const std::string dtype = shapes->value("_ArrayType_", std::string("int32"));
+        if (const Value* data = shapes->find("_ArrayData_")) {
+            const size_t n = domain.vol.size();
+            if (data->size() < n) throw std::runtime_error("_ArrayData_ holds fewer elements than _ArraySize_");
+            for (size_t i = 0; i < n; i++) domain.vol[i] = static_cast<int32_t>(data->at(i).as_int64());
+        } else if (const Value* zdata = shapes->find("_ArrayZipData_")) {
+            std::vector<unsigned char> zbuf;
+            if (zdata->is_string()) {
+                zbuf = base64_decode(zdata->as_string());
+            } else {
+                for (const Value& b : zdata->items()) zbuf.push_back(static_cast<unsigned char>(b.as_uint64()));
             }
+            const bool gzip = shapes->value("_ArrayZipType_", std::string("zlib")) == "gzip";
+            std::vector<unsigned char> raw = inflate_bytes(zbuf, gzip);
+            if (dtype == "uint8") copy_cast<uint8_t>(raw, domain.vol);
+            else if (dtype == "int8") copy_cast<int8_t>(raw, domain.vol);
+            else if (dtype == "uint16") copy_cast<uint16_t>(raw, domain.vol);
+            else if (dtype == "int16") copy_cast<int16_t>(raw, domain.vol);
+            else if (dtype == "uint32") copy_cast<uint32_t>(raw, domain.vol);
+            else copy_cast<int32_t>(raw, domain.vol);
+        }
+    } else {
+        // shape constructs (L537-570), compiled into ops one construct at a time and, unless the domain is built on
+        // the device (umcx_gpu_build_labels), painted on host threads before the next construct is read
+        const Value* first = shapes ? (shapes->is_array() ? &shapes->at(0) : shapes) : nullptr;
+        if (first) {
+            if (const Value* grid = first->find("Grid")) {
+                const Value& sz = grid->at("Size");
+                nx = static_cast<uint32_t>(sz.at(0).as_uint64());
+                ny = static_cast<uint32_t>(sz.at(1).as_uint64());
+                nz = static_cast<uint32_t>(sz.at(2).as_uint64());
+                grid_fill = grid->at("Tag").as_int();
+            }
+        }
+        if (domain_on_device) {
+            domain.nx = nx;
+            domain.ny = ny;
+            domain.nz = nz;
+            domain.vol.clear();
+        } else {
+            domain.reshape(nx, ny, nz, grid_fill);
+        }
+        auto paint = [&](size_t op_begin, size_t op_end) {
+            // z-slabs on host threads (every voxel is written by exactly one thread)
+            std::atomic<uint32_t> nextz{0};
+            std::atomic<bool> missing{false};
+            auto slabs = [&]() {
+                bool miss = false;
+                for (uint32_t z; !miss && (z = nextz.fetch_add(1)) < domain.nz;)
+                    for (uint32_t y = 0; y < domain.ny; y++)
+                        for (uint32_t x = 0; x < domain.nx; x++) {
+                            const int64_t idx = domain.index(static_cast<int>(x), static_cast<int>(y), static_cast<int>(z));
+                            const float px = x + 0.5f, py = y + 0.5f, pz = z + 0.5f;
+                            for (size_t k = op_begin; k < op_end; k++) {
+                                const int label = umcx_shape::eval_op(shape_ops[k], px, py, pz, &miss);
+                                if (label) domain.vol[static_cast<size_t>(idx)] = label;  // MCX_volume::mask, L138-140
+                            }
+                        }
+                if (miss) {
+                    missing.store(true);
+                    nextz.store(domain.nz);
+                }
+            };
+            const size_t nvox = static_cast<size_t>(domain.nx) * domain.ny * domain.nz;
+            unsigned nthr = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+            if (nvox < (1u << 16)) nthr = 1;
+            std::vector<std::thread> pool;
+            for (unsigned t = 1; t < nthr; t++) pool.emplace_back(slabs);
+            slabs();
+            for (auto& th : pool) th.join();
+            if (missing.load()) missing_number();
+        };
+        if (shapes) {
             std::vector<const Value*> objs;
             if (shapes->is_array()) {
                 for (const Value& o : shapes->items()) objs.push_back(&o);
@@ -532,71 +572,16 @@ void UserIO::initdomain() {
             }
             for (const Value* obj : objs) {
                 const std::string key = obj->is_object() && !obj->empty() ? obj->front_member().first : std::string();
-                CompiledShape cs;
-                if (compile_shape(key, obj->front_member().second, &cs)) {
-                    const bool layers = key.find("Layers") == 1;
-                    const size_t nl = layers ? cs.layers.size() : 1;
-                    // z-slabs on host threads (every voxel is written by exactly one thread)
-                    std::atomic<uint32_t> nextz{0};
-                    std::exception_ptr err;
-                    std::mutex err_mutex;
-                    auto slabs = [&]() {
-                        try {
-                            for (uint32_t z; (z = nextz.fetch_add(1)) < domain.nz;)
-                                for (uint32_t y = 0; y < domain.ny; y++)
-                                    for (uint32_t x = 0; x < domain.nx; x++) {
-                                        const int64_t idx = domain.index(static_cast<int>(x), static_cast<int>(y), static_cast<int>(z));
-                                        const P3 p{x + 0.5f, y + 0.5f, z + 0.5f};
-                                        for (size_t l = 0; l < nl; l++) {
-                                            const int label = eval_shape(cs, p, l);
-                                            if (label) domain.vol[static_cast<size_t>(idx)] = label;  // MCX_volume::mask, L138-140
-                                        }
-                                    }
-                        } catch (...) {
-                            std::lock_guard<std::mutex> lock(err_mutex);
-                            if (!err) err = std::current_exception();
-                            nextz.store(domain.nz);
-                        }
-                    };
-                    const size_t nvox = static_cast<size_t>(domain.nx) * domain.ny * domain.nz;
-                    unsigned nthr = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
-                    if (nvox < (1u << 16)) nthr = 1;
-                    std::vector<std::thread> pool;
-                    for (unsigned t = 1; t < nthr; t++) pool.emplace_back(slabs);
-                    slabs();
-                    for (auto& th : pool) th.join();
-                    if (err) std::rethrow_exception(err);
+                const size_t before = shape_ops.size();
+                if (compile_shape(key, obj->front_member().second, &shape_ops)) {
+                    if (!domain_on_device) paint(before, shape_ops.size());
                 } else if (!(key == "Name" || key == "Grid" || key == "Origin")) {
                     throw std::runtime_error("shape construct" + key + " is not supported");
                 }
             }
-        } else {  // JData volume (L571-598)
-            const Value& sz = shapes->at("_ArraySize_");
-            domain.reshape(static_cast<uint32_t>(sz.at(0).as_uint64()), static_cast<uint32_t>(sz.at(1).as_uint64()),
-                           static_cast<uint32_t>(sz.at(2).as_uint64()));
-            const std::string dtype = shapes->value("_ArrayType_", std::string("int32"));
-            if (const Value* data = shapes->find("_ArrayData_")) {
-                const size_t n = domain.vol.size();
-                if (data->size() < n) throw std::runtime_error("_ArrayData_ holds fewer elements than _ArraySize_");
-                for (size_t i = 0; i < n; i++) domain.vol[i] = static_cast<int32_t>(data->at(i).as_int64());
-            } else if (const Value* zdata = shapes->find("_ArrayZipData_")) {
-                std::vector<unsigned char> zbuf;
-                if (zdata->is_string()) {
-                    zbuf = base64_decode(zdata->as_string());
-                } else {
-                    for (const Value& b : zdata->items()) zbuf.push_back(static_cast<unsigned char>(b.as_uint64()));
-                }
-                const bool gzip = shapes->value("_ArrayZipType_", std::string("zlib")) == "gzip";
-                std::vector<unsigned char> raw = inflate_bytes(zbuf, gzip);
-                if (dtype == "uint8") copy_cast<uint8_t>(raw, domain.vol);
-                else if (dtype == "int8") copy_cast<int8_t>(raw, domain.vol);
-                else if (dtype == "uint16") copy_cast<uint16_t>(raw, domain.vol);
-                else if (dtype == "int16") copy_cast<int16_t>(raw, domain.vol);
-                else if (dtype == "uint32") copy_cast<uint32_t>(raw, domain.vol);
-                else copy_cast<int32_t>(raw, domain.vol);
-            }
         }
     }
+    if (domain_on_device) return;  // detectors are masked by the device label builder
     const Value* optode = cfg.find("Optode");
     if (optode && optode->contains("Detector")) maskdetectors(optode->at("Detector"));
 }
@@ -808,7 +793,9 @@ Job make_job(const UserIO& io) {
         for (int k = 0; k < 3; k++) o[k] = d.at("Pos").at(static_cast<size_t>(k)).as_float();
         o[3] = d.at("R").as_float();
     }
-    // labels: int32 + sign-bit detector flag -> uint8 + bit 7
+    // labels: int32 + sign-bit detector flag -> uint8 + bit 7 (built by umcx_gpu_build_labels instead when the
+    // domain is made on the device)
+    if (io.domain_on_device) return job;
     job.labels.resize(io.domain.vol.size());
     for (size_t i = 0; i < io.domain.vol.size(); i++) {
         const int32_t v = io.domain.vol[i];

@@ -33,8 +33,17 @@ public:
     Action action = Action::Run;
     std::string console;  // text the reference would print before exiting (help, --dumpjson)
 
+    // compiled shape constructs of the domain in input order (layers expanded), with the Grid fill value; empty
+    // for a JData volume (domain_is_volume), which is decoded into `domain` on the host
+    std::vector<umcx_shape_op> shape_ops;
+    int32_t grid_fill = 0;
+    bool domain_is_volume = false;
+    // true: shapes are not painted and detectors not masked on the host; `domain` keeps only the dimensions (and
+    // the decoded volume of a JData input) and umcx_gpu_build_labels builds the labels on the GPU
+    bool domain_on_device = false;
+
     // parse a reference command line (argv[0] is the program name), L474-532
-    UserIO(int argc, const char* const argv[]);
+    UserIO(int argc, const char* const argv[], bool device_domain = false);
     // JSON string input as MCX_run_json does (L853-856)
     static UserIO from_json(const std::string& json);
 

@@ -65,6 +65,19 @@ int batch_occupancy(bool reflect, int block, size_t smem);
 void launch_batch(int grid, int block, size_t smem, bool reflect, const BParams& BP, const KBuffers& B,
                   cudaStream_t st);
 
+// device label builder (raster.cu): one detector's half-voxel sampling lattice, coordinates at coords[off + i]
+struct DetLattice {
+    float x, y, z, r;  // detector centre and radius
+    unsigned xoff, yoff, zoff;
+    unsigned nxs, nys, nzs;
+};
+void launch_raster(const umcx_shape_op* ops, int nops, int32_t fill, const uint32_t dim[3], int32_t* vol,
+                   unsigned* missing, int sm_count, cudaStream_t stream);
+void launch_mask_det(const int32_t* vol, const uint32_t dim[3], const DetLattice& d, const float* coords,
+                     uint8_t* mark, int sm_count, cudaStream_t stream);
+void launch_finish_labels(const int32_t* vol, const uint8_t* mark, unsigned long long n, int mediumnum,
+                          uint8_t* out, unsigned long long* first_bad, int sm_count, cudaStream_t stream);
+
 void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream);
 
 void launch_rng_dump(const uint32_t seeds[4], unsigned long long offset, unsigned nphoton, unsigned ndraw, float* out,

@@ -121,13 +121,21 @@ int umcx_main(int argc, char* argv[]) {
 }
 
 int umcx_job_from_args(umcx_job** out, int argc, const char* const argv[]) {
+    return umcx_job_from_args_ex(out, argc, argv, 0u);
+}
+
+int umcx_job_from_args_ex(umcx_job** out, int argc, const char* const argv[], uint32_t flags) {
     if (!out) return UMCX_ERR_INPUT;
     *out = nullptr;
     umcx_job* j = new (std::nothrow) umcx_job();
     if (!j) return UMCX_ERR_INPUT;
     *out = j;
+    if (flags & ~UMCX_JOB_DEVICE_LABELS) {
+        j->err = "unknown umcx_job_from_args_ex flags";
+        return UMCX_ERR_INPUT;
+    }
     try {
-        j->io.reset(new UserIO(argc, argv));
+        j->io.reset(new UserIO(argc, argv, (flags & UMCX_JOB_DEVICE_LABELS) != 0));
         j->action = static_cast<int>(j->io->action);
         j->console = j->io->console;
         if (j->io->action == Action::Run) j->job = umcx::make_job(*j->io);
@@ -148,7 +156,27 @@ const char* umcx_job_error(const umcx_job* j) { return j ? j->err.c_str() : "no 
 int umcx_job_action(const umcx_job* j) { return j ? j->action : -1; }
 const char* umcx_job_console(const umcx_job* j) { return j ? j->console.c_str() : ""; }
 const umcx_sim* umcx_job_sim(const umcx_job* j) { return j && j->io ? &j->job.sim : nullptr; }
-const uint8_t* umcx_job_labels(const umcx_job* j) { return j ? j->job.labels.data() : nullptr; }
+const uint8_t* umcx_job_labels(const umcx_job* j) {
+    return j && !j->job.labels.empty() ? j->job.labels.data() : nullptr;
+}
+
+int umcx_job_build_labels(const umcx_job* j, umcx_context* ctx, uint8_t* d_labels) {
+    if (!j || !j->io || j->action != static_cast<int>(Action::Run) || !ctx || !d_labels) return UMCX_ERR_INPUT;
+    const UserIO& io = *j->io;
+    umcx_domain dom;
+    std::memset(&dom, 0, sizeof(dom));
+    dom.dim[0] = io.domain.nx;
+    dom.dim[1] = io.domain.ny;
+    dom.dim[2] = io.domain.nz;
+    dom.fill = io.grid_fill;
+    dom.ops = io.shape_ops.data();
+    dom.nops = static_cast<int32_t>(io.shape_ops.size());
+    dom.mediumnum = j->job.sim.mediumnum;
+    dom.volume = io.domain_is_volume ? io.domain.vol.data() : nullptr;
+    dom.detpos = j->job.detpos.data();
+    dom.detnum = j->job.sim.detnum;
+    return umcx_gpu_build_labels(ctx, &dom, d_labels);
+}
 const float* umcx_job_media(const umcx_job* j) { return j ? j->job.media.data() : nullptr; }
 const float* umcx_job_detpos(const umcx_job* j) { return j ? j->job.detpos.data() : nullptr; }
 int umcx_job_isnormalized(const umcx_job* j) { return j ? j->job.isnormalized : 0; }
@@ -159,7 +187,7 @@ const char* umcx_job_config_json(const umcx_job* j, int indent) {
     return buf.c_str();
 }
 int umcx_job_domain_int32(const umcx_job* j, int32_t* out, size_t n) {
-    if (!j || !j->io || !out) return UMCX_ERR_INPUT;
+    if (!j || !j->io || !out || j->io->domain_on_device) return UMCX_ERR_INPUT;
     if (n < j->io->domain.vol.size()) return UMCX_ERR_INPUT;
     std::memcpy(out, j->io->domain.vol.data(), j->io->domain.vol.size() * sizeof(int32_t));
     return UMCX_OK;
@@ -197,7 +225,7 @@ int umcx_job_write_outputs(const umcx_job* j, const float* fluence, const float*
     }
 }
 int umcx_job_dump_mask(const umcx_job* j, const char* path) {
-    if (!j || !j->io || !path) return UMCX_ERR_INPUT;
+    if (!j || !j->io || !path || j->io->domain_on_device) return UMCX_ERR_INPUT;
     try {
         j->io->save_volume_i32(j->io->domain, path);
         return UMCX_OK;

@@ -51,8 +51,9 @@ def config5(i: int, photon_scale: float = 1.0, max_edge: int | None = None) -> d
     }
 
 
-def batch5(n: int = 256, photon_scale: float = 1.0, max_edge: int | None = None):
-    """Jobs of the batched benchmark (umcx_gb300.Job objects)."""
+def batch5(n: int = 256, photon_scale: float = 1.0, max_edge: int | None = None, device_labels: bool = False):
+    """Jobs of the batched benchmark (umcx_gb300.Job objects); device_labels=True leaves the label volumes to be
+    built on the GPU (Batch.from_jobs(..., device_labels=True))."""
     from .api import Job
 
-    return [Job.from_json(config5(i, photon_scale, max_edge)) for i in range(n)]
+    return [Job.from_json(config5(i, photon_scale, max_edge), device_labels) for i in range(n)]
