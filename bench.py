@@ -212,32 +212,55 @@ def measure_batched(ctx, args, device) -> dict:
     from umcx_gb300.api import Batch, autotune_batch
     from umcx_gb300.workloads import batch5
 
-    jobs = batch5(args.batch_sims, photon_scale=args.batch_scale)
+    # set-up cost: JSON -> jobs -> batch, with the label volumes painted on the host or built on the GPU
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = Batch.from_jobs(ctx, batch5(args.batch_sims, photon_scale=args.batch_scale))
+    torch.cuda.synchronize()
+    setup_host = time.perf_counter() - t0
+    b.close()
+    t0 = time.perf_counter()
+    jobs = batch5(args.batch_sims, photon_scale=args.batch_scale, device_labels=True)
+    b = Batch.from_jobs(ctx, jobs, device_labels=True)
+    torch.cuda.synchronize()
+    setup_device = time.perf_counter() - t0
     n = sum(j.sim.nphoton for j in jobs)
     tune = autotune_batch(ctx, jobs, fraction=0.2, min_photons=500,
                           candidates=((512, 1), (1024, 1), (512, 2), (1024, 2)))
-    b = Batch.from_jobs(ctx, jobs)
     b.set_tuning(tune["block_size"], tune["blocks_per_sm"], tune["aggregation"])
     b.run()
     runs = [b.run() for _ in range(2)]
     ms = statistics.mean(r.kernel_ms for r in runs)
     steps_per_photon = runs[-1].steps / max(1, runs[-1].launched)
+    # end to end: one more run plus every simulation's output volume read back to the host
+    t0 = time.perf_counter()
+    b.run()
+    out_bytes = 0
+    for i in range(len(jobs)):
+        flu, _ = b.get(i)
+        out_bytes += 0 if flu is None else flu.nbytes
+    run_get = time.perf_counter() - t0
     b.close()
     # the same simulations one launch each (device buffers, same tuning)
     ctx.set_tuning(tune["block_size"], tune["blocks_per_sm"], tune["aggregation"])
     biggest = max(j.sim.dim[0] * j.sim.dim[1] * j.sim.dim[2] * j.sim.dim[3] for j in jobs)
     d_flu = torch.empty(biggest, dtype=torch.float32, device=f"cuda:{device}")
+    d_lab = torch.empty(max(j.sim.dim[0] * j.sim.dim[1] * j.sim.dim[2] for j in jobs), dtype=torch.uint8,
+                        device=f"cuda:{device}")
     stream = torch.cuda.current_stream()
     seq = 0.0
     for j in jobs:
-        d_lab = torch.from_numpy(j.labels.ravel().copy()).to(f"cuda:{device}")
+        j.build_labels(ctx, d_lab)
         seq += ctx.forward_device(j.sim, d_lab, j.media, None, d_flu, None, stream).kernel_ms
     ctx.set_tuning()
     return {"workload": f"{len(jobs)} simulations, edges 32-128, 2-5 labels, log-uniform 1e5-1e7 photons "
                         f"(x{args.batch_scale}), 10 gates",
             "photons": n, "steps_per_photon": steps_per_photon,
             "photons_per_ms": n / ms, "graph_ms": ms, "sequential_photons_per_ms": n / seq,
-            "sequential_kernel_ms": seq, "speedup_vs_sequential": seq / ms, "tuning": tune}
+            "sequential_kernel_ms": seq, "speedup_vs_sequential": seq / ms, "tuning": tune,
+            "setup_s": {"labels_on_host": setup_host, "labels_on_gpu": setup_device},
+            "e2e": {"photons_per_ms": n / ((setup_device + run_get) * 1e3), "setup_s": setup_device,
+                    "run_and_readback_s": run_get, "d2h_bytes": out_bytes}}
 
 
 def run_gpu_arm(args) -> None:

@@ -84,6 +84,10 @@ class Job:
             return None
         return np.ctypeslib.as_array(p, shape=(n,)).copy().reshape(s.dim[0], s.dim[1], s.dim[2])
 
+    @property
+    def has_host_labels(self) -> bool:
+        return bool(load().umcx_job_labels(self._h))
+
     def build_labels(self, ctx: "Context", d_labels) -> None:
         """Build this job's uint8 label volume on the GPU (umcx_job_build_labels) into d_labels: a CUDA tensor of
         nx*ny*nz bytes, or a device address (int)."""
@@ -324,12 +328,14 @@ class Batch:
         self.sims = [s.copy() for s in sims]
 
     @classmethod
-    def from_jobs(cls, ctx: Context, jobs, device_labels: bool = False) -> "Batch":
-        """Batch of parsed jobs.  device_labels=True builds every label volume on the GPU straight into the batch's
-        label pool (umcx_job_build_labels at umcx_batch_labels), with no host volume at all."""
+    def from_jobs(cls, ctx: Context, jobs, device_labels: bool = False, sims=None) -> "Batch":
+        """Batch of parsed jobs (sims: replacement simulation descriptions, e.g. with scaled photon counts).
+        device_labels=True builds every label volume on the GPU straight into the batch's label pool
+        (umcx_job_build_labels at umcx_batch_labels), with no host volume at all."""
+        sims = [j.sim for j in jobs] if sims is None else sims
         if not device_labels:
-            return cls(ctx, [j.sim for j in jobs], [j.labels for j in jobs], [j.media for j in jobs])
-        b = cls(ctx, [j.sim for j in jobs], None, [j.media for j in jobs])
+            return cls(ctx, sims, [j.labels for j in jobs], [j.media for j in jobs])
+        b = cls(ctx, sims, None, [j.media for j in jobs])
         for i, j in enumerate(jobs):
             j.build_labels(ctx, b.label_ptr(i))
         return b
@@ -379,7 +385,7 @@ def autotune_batch(ctx: Context, jobs, fraction: float = 0.05,
         s = j.sim
         s.nphoton = min(s.nphoton, max(min_photons, int(s.nphoton * fraction)))
         sims.append(s)
-    probe = Batch(ctx, sims, [j.labels for j in jobs], [j.media for j in jobs])
+    probe = Batch.from_jobs(ctx, jobs, device_labels=not all(j.has_host_labels for j in jobs), sims=sims)
     best = None
     for block, agg in candidates:
         probe.set_tuning(block, 0, agg)
