@@ -296,9 +296,11 @@ def run_gpu_arm(args) -> None:
     tuning = {"block_size": args.block, "blocks_per_sm": args.blocks_per_sm, "aggregation": args.aggregation,
               "source": "command line"}
     if not (args.block or args.blocks_per_sm or args.aggregation) and not args.no_autotune:
-        # the project's autotuner: short timed runs (10 % of the photons) over block sizes and aggregation modes
-        tuning = dict(ctx.autotune(sim, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.1),
-                      source="autotune (10 % photon probes)")
+        # the project's autotuner: timed runs at half the photons over block sizes and aggregation modes.  A probe
+        # must be long against the launch's drain (the last, longest photons: ~8 ms here), or the drain's noise
+        # decides the choice
+        tuning = dict(ctx.autotune(sim, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.5),
+                      source="autotune (50 % photon probes)")
 
     def barrier():
         if ws > 1:

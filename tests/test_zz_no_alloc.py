@@ -59,8 +59,9 @@ def test_noalloc_matches_allocating_entry_point_twice():
                                                                           ref.detected), call
         assert abs(res.energy_total - ref.energy_total) <= 1e-9 * ref.energy_total
         assert abs(res.energy_escape - ref.energy_escape) <= 1e-9 * ref.energy_total
-        # atomic accumulation order differs between runs: FP32 rounding tolerance
-        np.testing.assert_allclose(flu.cpu().numpy(), ref_flu_h, rtol=1e-4, atol=1e-6)
+        # atomic accumulation order differs between runs: FP32 rounding of long sums (the source voxel collects
+        # ~1e5 deposits into a value near 2e5, whose ulp is 1/64, so the order alone moves it by up to ~2e-4)
+        np.testing.assert_allclose(flu.cpu().numpy(), ref_flu_h, rtol=1e-3, atol=1e-6)
         rows = dp.cpu().numpy()[: res.saved * cols].reshape(-1, cols)
         ref_rows = ref_det.cpu().numpy()[: ref.saved * cols].reshape(-1, cols)
         order = np.lexsort(rows.T[::-1])

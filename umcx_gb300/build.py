@@ -47,6 +47,11 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+def _extra_defs() -> list[str]:
+    """Extra -D definitions for nvcc from UMCX_NVCC_DEFS (space separated), for build variants."""
+    return [f"-D{d}" for d in os.environ.get("UMCX_NVCC_DEFS", "").split() if d]
+
+
 def _have_zlib() -> bool:
     return Path("/usr/include/zlib.h").exists() and any(
         Path(d, n).exists()
@@ -85,7 +90,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         obj = OUT / (unit + ".o")
         objs.append(obj)
         if _stale(obj, [src, *hdrs]):
-            steps.append(([nvcc, *NVCC_FLAGS, *ARCH, *extra, "-c", str(src), "-o", str(obj)], OUT / (unit + ".log")))
+            steps.append(([nvcc, *NVCC_FLAGS, *ARCH, *extra, *_extra_defs(), "-c", str(src), "-o", str(obj)],
+                          OUT / (unit + ".log")))
     for unit in CPP_UNITS:
         src = CSRC / unit
         obj = OUT / (unit + ".o")

@@ -524,11 +524,11 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         B.grad = static_cast<double*>(ctx->grad.ptr);
         int block = ctx->tuning.block_size > 0 ? ctx->tuning.block_size : 256;
         size_t smem = adjoint_smem(P, block);
-        while (smem > 227 * 1024 && block > 32) {
+        while (smem > kMaxDynamicSmem && block > 32) {
             block /= 2;
             smem = adjoint_smem(P, block);
         }
-        if (smem > 227 * 1024) throw InputError("too many media for the adjoint's per-thread tallies");
+        if (smem > kMaxDynamicSmem) throw InputError("too many media for the adjoint's per-thread tallies");
         int occ = adjoint_occupancy(s->isreflect != 0, block, smem);
         if (occ < 1) occ = 1;
         int grid = ctx->sm_count * occ;
@@ -816,7 +816,7 @@ void batch_plan(umcx_batch* b) {
     for (auto& ch : b->chunks) {
         const int block = b->tuning.block_size > 0 ? b->tuning.block_size : 512;
         const size_t smem = batch_smem(ch.count, ch.total_media, block);
-        if (smem > 227 * 1024) throw InputError("batch chunk does not fit shared memory at this block size");
+        if (smem > kMaxDynamicSmem) throw InputError("batch chunk does not fit shared memory at this block size");
         int occ = batch_occupancy(b->reflect, block, smem);
         if (occ < 1) occ = 1;
         const int per_sm = b->tuning.blocks_per_sm > 0 ? std::min(b->tuning.blocks_per_sm, occ) : occ;

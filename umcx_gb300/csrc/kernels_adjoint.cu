@@ -11,8 +11,8 @@ size_t adjoint_smem(const KParams& P, int block) {
 }
 
 cudaError_t configure_adjoint_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_adjoint<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaError_t e = allow_max_dynamic_smem(k_adjoint<false>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_adjoint<true>);
     return e;
 }
 

@@ -9,8 +9,8 @@ size_t batch_smem(int nsim, int total_media, int block) {
 }
 
 cudaError_t configure_batch_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaError_t e = allow_max_dynamic_smem(k_batch<false>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_batch<true>);
     return e;
 }
 

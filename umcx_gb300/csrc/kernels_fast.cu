@@ -32,10 +32,10 @@ static int occ_one(int block, size_t smem) {
     return n;
 }
 
-// allow the forward kernels up to 227 KB of dynamic shared memory (large per-thread partial-path scratch)
+// allow the forward kernels all the dynamic shared memory a CTA can have (large per-thread partial-path scratch)
 template <bool R, bool D>
 static cudaError_t allow_big_smem() {
-    cudaError_t e = cudaFuncSetAttribute(k_forward<false, R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D>);
     // prefer L1 over shared memory: the label volume is read through L1 at every voxel crossing
     const char* pref = std::getenv("UMCX_SMEM_CARVEOUT");  // percent of the unified L1/shared array given to shared
     const int carve = pref ? std::atoi(pref) : kDefaultCarveout;
@@ -85,6 +85,10 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     lc.block = t.block_size > 0 ? t.block_size : 256;
     lc.aggregate = t.aggregation == 2 ? 1 : 0;
     lc.smem = forward_smem(P, lc.block, lc.savedet, 0);
+    while (lc.smem > kMaxDynamicSmem && lc.block > 32) {  // per-lane partial paths of many media: smaller CTAs
+        lc.block /= 2;
+        lc.smem = forward_smem(P, lc.block, lc.savedet, 0);
+    }
     int occ = forward_occupancy(strict, lc.reflect, lc.savedet, lc.block, lc.smem);
     if (occ < 1) occ = 1;
     int per_sm = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
@@ -93,7 +97,7 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     const int bits = P.palette_bits;
     if (!strict && bits > 0 && P.packed_words > 0 && t.label_pack == 2) {
         const size_t smem = forward_smem(P, lc.block, lc.savedet, bits);
-        int occ_p = smem <= 227u * 1024u ? occupancy_packed(lc.reflect, lc.savedet, bits, lc.block, smem) : 0;
+        int occ_p = smem <= kMaxDynamicSmem ? occupancy_packed(lc.reflect, lc.savedet, bits, lc.block, smem) : 0;
         const int per_sm_p = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ_p) : occ_p;
         if (per_sm_p >= 1) {
             lc.pack = bits;

@@ -50,7 +50,7 @@ int occupancy_packed(bool reflect, bool savedet, int pack, int block, size_t sme
 
 template <bool R, bool D, int K>
 static cudaError_t allow_big_smem() {
-    return cudaFuncSetAttribute(k_forward<false, R, D, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    return allow_max_dynamic_smem(k_forward<false, R, D, K>);
 }
 
 cudaError_t configure_packed_kernels() {

@@ -13,7 +13,7 @@ static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers&
 
 template <bool R, bool D>
 static cudaError_t allow_big_smem() {
-    return cudaFuncSetAttribute(k_forward<true, R, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    return allow_max_dynamic_smem(k_forward<true, R, D>);
 }
 cudaError_t configure_strict_kernels() {
     cudaError_t e = allow_big_smem<false, false>();

@@ -8,6 +8,19 @@
 
 namespace umcx_dev {
 
+// Let a kernel use all the dynamic shared memory a CTA may opt in to, less its static shared memory.
+template <class Kernel>
+inline cudaError_t allow_max_dynamic_smem(Kernel kernel) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    const int dyn = optin - static_cast<int>(fa.sharedSizeBytes);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn > 0 ? dyn : 0);
+}
+
 struct LaunchChoice {
     int block = 256;
     int grid = 0;

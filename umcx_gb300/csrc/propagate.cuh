@@ -179,10 +179,12 @@ struct Photon {
 // parameter) or SimDesc (one simulation of a batch, shared memory); both expose the same member names.
 template <class PV>
 __device__ __forceinline__ int vox_index(const PV& P, int ix, int iy, int iz) {  // L128-130
-    return (ix < 0 || iy < 0 || iz < 0 || ix >= P.nx || iy >= P.ny || iz >= P.nz)
-               ? -1
-               : static_cast<int>(static_cast<unsigned>(ix) * P.dimyz + static_cast<unsigned>(iy) * static_cast<unsigned>(P.nz) +
-                                  static_cast<unsigned>(iz));
+    // one unsigned compare per axis covers both bounds
+    return (static_cast<unsigned>(ix) < static_cast<unsigned>(P.nx) && static_cast<unsigned>(iy) < static_cast<unsigned>(P.ny) &&
+            static_cast<unsigned>(iz) < static_cast<unsigned>(P.nz))
+               ? static_cast<int>(static_cast<unsigned>(ix) * P.dimyz + static_cast<unsigned>(iy) * static_cast<unsigned>(P.nz) +
+                                  static_cast<unsigned>(iz))
+               : -1;
 }
 
 // rotatevector, L418-428
@@ -324,9 +326,10 @@ __device__ __forceinline__ bool skip_to_grid(const PV& P, Photon& p) {
 // *seg returns the distance moved.
 template <bool STRICT, class PV>
 __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, bool* crossed, float* moved) {
-    const float hx = fabsf((static_cast<float>(p.ix + (p.vx > 0.f)) - p.px) * p.rx);
-    const float hy = fabsf((static_cast<float>(p.iy + (p.vy > 0.f)) - p.py) * p.ry);
-    const float hz = fabsf((static_cast<float>(p.iz + (p.vz > 0.f)) - p.pz) * p.rz);
+    const int bx = p.vx > 0.f, by = p.vy > 0.f, bz = p.vz > 0.f;
+    const float hx = fabsf((static_cast<float>(p.ix + bx) - p.px) * p.rx);
+    const float hy = fabsf((static_cast<float>(p.iy + by) - p.py) * p.ry);
+    const float hz = fabsf((static_cast<float>(p.iz + bz) - p.pz) * p.rz);
     float dist = fminf(fminf(hx, hy), hz);
     p.flip = (dist == hx ? 0 : (dist == hy ? 1 : 2));
     const float mus = m.a.y;
@@ -351,13 +354,13 @@ __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, boo
     }
     p.lz += dist;
     *moved = dist;
-    if (*crossed) {
-        if (p.flip == 0) p.ix += (p.vx > 0.f ? 1 : -1);
-        else if (p.flip == 1) p.iy += (p.vy > 0.f ? 1 : -1);
-        else p.iz += (p.vz > 0.f ? 1 : -1);
-        return vox_index(P, p.ix, p.iy, p.iz);
-    }
-    return p.lastvox;
+    // branch-free voxel update: +-1 on the crossed axis only
+    const int f = p.flip;
+    const int c = *crossed;
+    p.ix += (c & (f == 0)) * (2 * bx - 1);
+    p.iy += (c & (f == 1)) * (2 * by - 1);
+    p.iz += (c & (f == 2)) * (2 * bz - 1);
+    return c ? vox_index(P, p.ix, p.iy, p.iz) : p.lastvox;
 }
 
 // MCX_photon::scatter, L364-380
@@ -379,14 +382,13 @@ __device__ __forceinline__ void scatter(Photon& p, const Medium& m) {
         stheta = sinf(th);
         ctheta = cosf(th);
     } else {
-        if (fabsf(g) > FLT_EPSILON) {
-            const float t = __fdividef(m.c.x, m.c.y + m.c.z * rng_rand01(p.rng));
-            ctheta = (m.c.w - t * t) * m.b.z;
-        } else {
-            ctheta = 2.f * rng_rand01(p.rng) - 1.f;
-        }
+        // both cases draw one number: select instead of branching (lanes in different media do not diverge)
+        const float r = rng_rand01(p.rng);
+        const float t = __fdividef(m.c.x, m.c.y + m.c.z * r);
+        ctheta = fabsf(g) > FLT_EPSILON ? (m.c.w - t * t) * m.b.z : 2.f * r - 1.f;
         ctheta = fmaxf(-1.f, fminf(1.f, ctheta));
-        stheta = sqrtf(fmaxf(0.f, 1.f - ctheta * ctheta));
+        const float s2 = fmaxf(0.f, 1.f - ctheta * ctheta);
+        stheta = s2 > 0.f ? s2 * rsqrtf(s2) : 0.f;
     }
     rotate<STRICT>(p, stheta, ctheta, sphi, cphi);
     p.rx = rcp_<STRICT>(p.vx);
@@ -480,8 +482,28 @@ __global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict
 
 // =============================================================================================== loop building blocks
 struct Counters {
-    unsigned launch = 0, steps = 0, cross = 0, scat = 0, refl = 0, cap = 0;
+    unsigned steps = 0, cross = 0, scat = 0;
 };
+
+// Per-CTA counts of rare events (photon launches, reflections, photons stopped by a guard), kept with shared-memory
+// atomics so that they take no registers in the hot loop.  Every kernel resets them before its first barrier and
+// adds them to the launch's statistics after its loop (rare_flush, reached by all threads).
+enum { kRareLaunch = 0, kRareRefl = 1, kRareCap = 2 };
+static __shared__ unsigned long long s_rare[3];
+__device__ __forceinline__ void rare_reset() {
+    if (threadIdx.x < 3) s_rare[threadIdx.x] = 0ULL;
+}
+__device__ __forceinline__ void rare_count(int k) { atomicAdd(&s_rare[k], 1ULL); }
+
+// launch deadline of the CTA (wall clock, %globaltimer), set by thread 0 before the kernel's first barrier
+static __shared__ unsigned long long s_tend;
+
+// dynamic shared memory a propagation kernel's CTA can have next to the engine's static shared memory
+// (the prefetched photon indices, the rare-event counts and the deadline), with room for alignment
+constexpr size_t kMaxDynamicSmem = 227u * 1024u - (1024u * 8u + 3u * 8u + 8u) - 256u;
+__device__ __forceinline__ void set_deadline(unsigned long long budget_ns) {
+    if (threadIdx.x == 0) s_tend = global_ns() + budget_ns;
+}
 
 // what one loop iteration did to an active photon
 struct Event {
@@ -561,7 +583,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
         else p.media &= 0xFFFFu;
         if (++p.nsteps > P.step_cap || p.media >= (kZeroStepLimit << 16)) {
             ev.term = true;
-            c.cap++;
+            rare_count(kRareCap);
         } else if (newvox != p.lastvox) {
             c.cross++;
             ev.crossed = true;
@@ -569,8 +591,9 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
             ev.left_mid = mid;
             ev.seg = p.lz;
             ev.w_before = p.lw;
-            ev.gate = static_cast<int>(fminf(static_cast<float>(P.maxgate - 1),
-                                             static_cast<float>(static_cast<int>(floorf((p.ly - P.tstart) * P.rtstep)))));
+            // (int)fminf(maxgate - 1, floorf(x)) as one rounding conversion and an integer min (same value for
+            // every x: the conversion saturates like the reference's cast chain does on the device)
+            ev.gate = min(__float2int_rd((p.ly - P.tstart) * P.rtstep), P.maxgate - 1);
             ev.dep_val = deposit_value<STRICT>(P, p, m);
             if (RESET_SEGMENT || P.issavevol) {
                 p.lw = p.pw;
@@ -582,7 +605,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
                 unsigned newmedia = (newvox >= 0) ? labels(newvox) : 0u;
                 const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
                 if (REFLECT && P.isreflect && m.a.w != n2) {
-                    c.refl++;
+                    rare_count(kRareRefl);
                     if (reflect<STRICT>(p, m.a.w, n2)) {
                         if (newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0) ev.term = true;
                     } else {
@@ -609,21 +632,23 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
 
 // per-lane photon indices: the first is the lane's global index, the next one is fetched from the global counter
 // when the current one starts, so the atomic's latency overlaps the photon's whole life
-// (indices [0, lanes) are the lanes' first photons; counter value c stands for photon lanes + c)
+// (indices [0, lanes) are the lanes' first photons; counter value c stands for photon lanes + c).  The prefetched
+// index is touched once per photon and lives in shared memory, not in the hot loop's registers.
+static __shared__ unsigned long long s_next[1024];
 struct PhotonFeed {
-    unsigned long long next;
     __device__ __forceinline__ void init(unsigned long long* counter, unsigned long long gid, unsigned long long total,
                                          unsigned long long lanes) {
         (void)counter;
         (void)total;
         (void)lanes;
-        next = gid;
+        s_next[threadIdx.x] = gid;
     }
     // false when no photon is left; otherwise returns the prefetched index and prefetches the following one
     __device__ __forceinline__ bool take(unsigned long long* counter, unsigned long long* idx, unsigned long long n) {
+        const unsigned long long next = s_next[threadIdx.x];
         if (next >= n) return false;
         *idx = next;
-        next = atomicAdd(counter, 1ULL) + static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+        s_next[threadIdx.x] = atomicAdd(counter, 1ULL) + static_cast<unsigned long long>(gridDim.x) * blockDim.x;
         return true;
     }
 };
@@ -701,38 +726,43 @@ __device__ __forceinline__ void flush_tallies(const KBuffers& B, unsigned lane, 
     for (int off = 16; off > 0; off >>= 1) {
         tot += __shfl_down_sync(kFull, tot, off);
         esc += __shfl_down_sync(kFull, esc, off);
-        c.launch += __shfl_down_sync(kFull, c.launch, off);
         c.steps += __shfl_down_sync(kFull, c.steps, off);
         c.cross += __shfl_down_sync(kFull, c.cross, off);
         c.scat += __shfl_down_sync(kFull, c.scat, off);
-        c.refl += __shfl_down_sync(kFull, c.refl, off);
-        c.cap += __shfl_down_sync(kFull, c.cap, off);
     }
     if (lane == 0) {
         atomicAdd(&B.stats->total, tot);
         atomicAdd(&B.stats->escape, esc);
-        atomicAdd(&B.stats->launched, static_cast<unsigned long long>(c.launch));
         atomicAdd(&B.stats->steps, static_cast<unsigned long long>(c.steps));
         atomicAdd(&B.stats->crossings, static_cast<unsigned long long>(c.cross));
         atomicAdd(&B.stats->scatters, static_cast<unsigned long long>(c.scat));
-        atomicAdd(&B.stats->reflections, static_cast<unsigned long long>(c.refl));
-        if (c.cap) atomicAdd(&B.stats->capped, static_cast<unsigned long long>(c.cap));
+    }
+}
+
+// the CTA's rare-event counts into the launch statistics; every thread of the CTA must call it
+__device__ __forceinline__ void rare_flush(const KBuffers& B) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(&B.stats->launched, s_rare[kRareLaunch]);
+        atomicAdd(&B.stats->reflections, s_rare[kRareRefl]);
+        if (s_rare[kRareCap]) atomicAdd(&B.stats->capped, s_rare[kRareCap]);
     }
 }
 
 // copies the media table (3 float4 per medium) into shared memory
 __device__ __forceinline__ void load_media(const KParams& P, const Medium* src, Medium* sm) {
+    rare_reset();
+    set_deadline(P.budget_ns);
     const float4* s = reinterpret_cast<const float4*>(src);
     float4* d = reinterpret_cast<float4*>(sm);
     for (int k = threadIdx.x; k < 3 * P.mediumnum; k += blockDim.x) d[k] = s[k];
     __syncthreads();
 }
 
-// uniform exit of a warp when the launch's wall-clock budget is used up
-__device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, unsigned lane,
-                                              unsigned long long t_end) {
+// uniform exit of a warp when the launch's wall-clock budget (deadline s_tend) is used up
+__device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, unsigned lane) {
     if ((iter & 1023u) != 0u) return false;
-    const bool late = global_ns() > t_end;
+    const bool late = global_ns() > s_tend;
     if (__any_sync(kFull, late)) {
         if (lane == 0) atomicExch(&B.stats->error, UMCX_ERR_TIMEOUT);
         return true;
@@ -752,8 +782,15 @@ struct LabelViewOf<0> {
 };
 
 // PACK = 0 reads labels from global memory; PACK = 2 or 4 reads the palette-packed copy staged in shared memory
+// launch bounds of the forward kernel (a build variant can trade resident lanes for registers, e.g.
+// UMCX_NVCC_DEFS="UMCX_FWD_THREADS=256 UMCX_FWD_MINB=3"; measured on GB300 the default 1024 x 1 at 64 registers is
+// as fast as 768 lanes at 74 registers and faster than 512 lanes at 86)
+#ifndef UMCX_FWD_THREADS
+#define UMCX_FWD_THREADS 1024
+#define UMCX_FWD_MINB 1
+#endif
 template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0>
-__global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffers B) {
+__global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
     // them out of the register budget of the hot loop
@@ -782,7 +819,6 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + tid, P.nphoton,
               static_cast<unsigned long long>(gridDim.x) * blockDim.x);
-    const unsigned long long t_end = global_ns() + P.budget_ns;
     Photon p;
     p.media = 0;
     p.lastvox = -1;
@@ -795,7 +831,7 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
             if (!feed.take(B.counter, &k, P.nphoton)) {
                 done = true;
             } else {
-                c.launch++;
+                rare_count(kRareLaunch);
                 active = start_photon<STRICT>(P, labels, p, P.photon_offset + k);
                 lwbuf[tid] = p.launchw;
                 if (SAVEDET && active)
@@ -803,7 +839,7 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
             }
         }
         if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane, t_end)) break;
+        if (out_of_budget(B, iter, lane)) break;
 
         int dep_idx = -1;
         float dep_val = 0.f;
@@ -811,14 +847,11 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
         ev.term = false;
         if (active) {
             advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c);
-            if (ev.crossed) {
-                if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.left_mid > 0)
-                    ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
-                if (P.issavevol && ev.gate >= 0) {
-                    dep_idx = ev.left_vox + ev.gate * static_cast<int>(P.dimxyz);
-                    dep_val = ev.dep_val;
-                }
-            }
+            if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0)
+                ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
+            const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
+            dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
+            dep_val = dep ? ev.dep_val : 0.f;
         }
         deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
         if (SAVEDET) {
@@ -836,6 +869,7 @@ __global__ void __launch_bounds__(1024) k_forward(const KParams P, const KBuffer
         }
     }
     flush_tallies(B, lane, tally[tid], tally[blockDim.x + tid], c);
+    rare_flush(B);
 }
 
 // =============================================================================================== adjoint kernel
@@ -878,7 +912,6 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * bd + tid, P.nphoton,
               static_cast<unsigned long long>(gridDim.x) * bd);
-    const unsigned long long t_end = global_ns() + P.budget_ns;
     Photon p;
     p.media = 0;
     p.lastvox = -1;
@@ -894,7 +927,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             if (!feed.take(B.counter, &k, P.nphoton)) {
                 done = true;
             } else {
-                c.launch++;
+                rare_count(kRareLaunch);
                 cur = P.photon_offset + k;
                 active = start_photon<false>(P, GlobalLabels{B.labels}, p, cur);
                 if (active) {
@@ -912,7 +945,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             }
         }
         if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane, t_end)) break;
+        if (out_of_budget(B, iter, lane)) break;
 
         int dep_idx = -1;
         float dep_val = 0.f;
@@ -991,6 +1024,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
         }
     }
     flush_tallies(B, lane, tot, esc, c);
+    rare_flush(B);
     // per-label gradient accumulators: warp reduction in FP64, one atomic per warp and label
     for (int q = 0; q < K; q++) {
         double a = ga[q * bd + tid], s = gs[q * bd + tid];
@@ -1018,7 +1052,6 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x, B.replay_count,
               static_cast<unsigned long long>(gridDim.x) * blockDim.x);
-    const unsigned long long t_end = global_ns() + P.budget_ns;
     Photon p;
     p.media = 0;
     p.lastvox = -1;
@@ -1035,13 +1068,13 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
                 done = true;
             } else {
                 rec = B.replay_list[k];
-                c.launch++;
+                rare_count(kRareLaunch);
                 active = start_photon<false>(P, GlobalLabels{B.labels}, p, rec.photon);
                 if (!active) mismatch++;
             }
         }
         if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane, t_end)) break;
+        if (out_of_budget(B, iter, lane)) break;
         if (active) {
             Event ev;
             advance<false, REFLECT, true>(P, GlobalLabels{B.labels}, sm, p, ev, c);
@@ -1059,6 +1092,7 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
     for (int off = 16; off > 0; off >>= 1) mismatch += __shfl_down_sync(kFull, mismatch, off);
     if (lane == 0 && mismatch) atomicAdd(&B.stats->capped, static_cast<unsigned long long>(mismatch));
     flush_tallies(B, lane, 0.0, 0.0, c);
+    rare_flush(B);
 }
 
 // =============================================================================================== batched kernel
@@ -1115,6 +1149,8 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         float4* md = reinterpret_cast<float4*>(sm);
         for (int k = threadIdx.x; k < 3 * BP.total_media; k += blockDim.x) md[k] = ms[k];
     }
+    rare_reset();
+    set_deadline(BP.budget_ns);
     __syncthreads();
 
     const unsigned tid = threadIdx.x;
@@ -1122,7 +1158,6 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + tid, BP.total,
               static_cast<unsigned long long>(gridDim.x) * blockDim.x);
-    const unsigned long long t_end = global_ns() + BP.budget_ns;
     Photon p;
     p.media = 0;
     p.lastvox = -1;
@@ -1154,12 +1189,12 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                     esc = 0.0;
                 }
                 const SimDesc& S = sd[sim];
-                c.launch++;
+                rare_count(kRareLaunch);
                 active = start_photon<false>(S, GlobalLabels{B.labels + S.label_off}, p, S.photon_offset + (g - begin[sim]));
             }
         }
         if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane, t_end)) break;
+        if (out_of_budget(B, iter, lane)) break;
 
         long long dep_idx = -1;
         float dep_val = 0.f;
@@ -1206,6 +1241,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         atomicAdd(BP.tallies + 2 * tally_sim + 1, tot);
     }
     flush_tallies(B, lane, 0.0, 0.0, c);
+    rare_flush(B);
 }
 
 // detector readings and their per-label derivatives from the extended records (FP64 accumulation):
