@@ -225,8 +225,11 @@ def measure_batched(ctx, args, device) -> dict:
     torch.cuda.synchronize()
     setup_device = time.perf_counter() - t0
     n = sum(j.sim.nphoton for j in jobs)
-    tune = autotune_batch(ctx, jobs, fraction=0.2, min_photons=500,
-                          candidates=((512, 1), (1024, 1), (512, 2), (1024, 2)))
+    if args.no_autotune:
+        tune = {"block_size": 1024, "blocks_per_sm": 0, "aggregation": 1, "source": "fixed"}
+    else:
+        tune = autotune_batch(ctx, jobs, fraction=0.2, min_photons=500,
+                              candidates=((512, 1), (1024, 1), (512, 2), (1024, 2)))
     b.set_tuning(tune["block_size"], tune["blocks_per_sm"], tune["aggregation"])
     b.run()
     runs = [b.run() for _ in range(2)]
@@ -374,8 +377,10 @@ def run_gpu_arm(args) -> None:
     if rank == 0 and not args.no_cpu:
         cpu = cpu_reference_run(args.cpu_photons, os.cpu_count() or 1)
     forms = {}
-    if rank == 0 and not args.no_forms:
+    wanted = set() if args.no_forms else {f.strip() for f in args.forms.split(",") if f.strip()}
+    if rank == 0 and "adjoint" in wanted:
         forms["adjoint"] = measure_adjoint(ctx, args)
+    if rank == 0 and "batched" in wanted:
         forms["batched"] = measure_batched(ctx, args, device)
 
     if rank == 0:
@@ -434,10 +439,11 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--aggregation", type=int, default=0)
     ap.add_argument("--no-forms", action="store_true", help="skip the adjoint and batched forms")
-    ap.add_argument("--no-autotune", action="store_true", help="use the built-in launch defaults")
+    ap.add_argument("--forms", default="adjoint,batched", help="comma list of the extra forms to measure")
+    ap.add_argument("--no-autotune", action="store_true", help="use the built-in launch defaults (forms: fixed)")
     ap.add_argument("--batch-sims", type=int, default=256)
     ap.add_argument("--batch-scale", type=float, default=0.1,
-                    help="photon-budget scale of the batched form (1.0 = the full 5.4e8-photon batch, ~4 min/run)")
+                    help="photon-budget scale of the batched form (1.0 = the full 5.4e8-photon batch, ~5 s/run)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
