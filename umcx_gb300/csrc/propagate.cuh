@@ -838,8 +838,11 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
                     for (int q = 0; q < P.ppathlen; q++) ppath[q * blockDim.x + tid] = 0.f;
             }
         }
-        if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane)) break;
+        // warp-uniform exits, tested every 16 iterations (a finished lane idles for at most 15 more)
+        if ((iter & 15u) == 0u) {
+            if (__all_sync(kFull, done)) break;
+            if (out_of_budget(B, iter, lane)) break;
+        }
 
         int dep_idx = -1;
         float dep_val = 0.f;
@@ -854,14 +857,17 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
             dep_val = dep ? ev.dep_val : 0.f;
         }
         deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
-        if (SAVEDET) {
-            const bool tdet = ev.term && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
-            detect_converged(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
-                write_detp(P, B, p, ppath + tid, blockDim.x, d, slot);
-            });
-        }
-        if (ev.term) {  // energy tallies (L765-770)
-            if ((p.media & UMCX_LABEL_MASK) != 0u) {
+        if (ev.term) {
+            // detection (L276-278, L429-435): a few photons per thousand, so each lane appends its own records
+            // with one atomic per hit instead of a per-iteration warp vote
+            if (SAVEDET && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend) {
+                for (int d = 0; d < P.detnum; d++) {
+                    if (!det_hit(P.det[d], p)) continue;
+                    const unsigned long long slot = atomicAdd(&B.stats->detected, 1ULL);
+                    if (slot < P.maxdetphotons) write_detp(P, B, p, ppath + tid, blockDim.x, d, slot);
+                }
+            }
+            if ((p.media & UMCX_LABEL_MASK) != 0u) {  // energy tallies (L765-770)
                 tally[tid] += static_cast<double>(lwbuf[tid]);
                 tally[blockDim.x + tid] += static_cast<double>(p.pw);
             }
