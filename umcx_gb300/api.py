@@ -211,15 +211,24 @@ class Context:
         t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms, label_pack)
         check(load().umcx_set_tuning(self._h, C.byref(t)), self._h, "umcx_set_tuning")
 
-    def forward(self, sim: Sim, labels, media, detpos=None) -> Forward:
-        """Host-buffer forward simulation (umcx_gpu_forward)."""
+    def forward(self, sim: Sim, labels, media, detpos=None, fluence=None, detp=None) -> Forward:
+        """Host-buffer forward simulation (umcx_gpu_forward).  fluence / detp: optional caller-owned float32 output
+        arrays (nx*ny*nz*maxgate and maxdetphotons*columns elements) reused across calls instead of new ones."""
         lab = np.ascontiguousarray(labels, np.uint8)
         med = np.ascontiguousarray(media, np.float32)
         det = np.ascontiguousarray(detpos if detpos is not None else np.zeros((0, 4)), np.float32)
         nout = sim.dim[0] * sim.dim[1] * sim.dim[2] * sim.dim[3]
-        flu = np.zeros(nout, np.float32) if sim.issavevol else None
         cols = detp_columns(sim)
-        dp = np.zeros(max(1, sim.maxdetphotons * cols), np.float32) if sim.issavedet else None
+        ndp = max(1, sim.maxdetphotons * cols)
+        flu = dp = None
+        if sim.issavevol:
+            flu = np.zeros(nout, np.float32) if fluence is None else fluence.reshape(-1)
+            if flu.dtype != np.float32 or flu.size < nout or not flu.flags.c_contiguous:
+                raise ValueError("fluence must be a contiguous float32 array of nx*ny*nz*maxgate elements")
+        if sim.issavedet:
+            dp = np.zeros(ndp, np.float32) if detp is None else detp.reshape(-1)
+            if dp.dtype != np.float32 or dp.size < ndp or not dp.flags.c_contiguous:
+                raise ValueError("detp must be a contiguous float32 array of maxdetphotons*columns elements")
         res = Result()
         rc = load().umcx_gpu_forward(self._h, C.byref(sim), lab.ctypes.data, med.ctypes.data,
                                      det.ctypes.data if det.size else None,
@@ -227,7 +236,7 @@ class Context:
                                      None if dp is None else dp.ctypes.data, C.byref(res))
         check(rc, self._h, "umcx_gpu_forward")
         if flu is not None:
-            flu = flu.reshape(sim.dim[3], sim.dim[0], sim.dim[1], sim.dim[2])
+            flu = flu[:nout].reshape(sim.dim[3], sim.dim[0], sim.dim[1], sim.dim[2])
         if dp is not None:
             dp = dp[: res.saved * cols].reshape(res.saved, cols)
         return Forward(flu, dp, res)
