@@ -1,9 +1,9 @@
 """CPU oracle of the umcx photon-transport hot path -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs may use this package, and only
-as the checker or the timed CPU baseline.  The product (umcx_gb300/) never imports it.
+as the reference results that GPU outputs are compared with, or as the timed CPU baseline.  The product (umcx_gb300/) never imports it.
 
-Two checkers live here:
+Two reference implementations live here:
   * libumcx_oracle.so, a plain-C restatement of the reference's photon loop (umcx_oracle.c), pinned bit-for-bit
     against the reference's own outputs (tests/test_oracle_pin.py);
   * oracle/_ref/umcx, the UNMODIFIED reference program built from its sources by build_ref.sh (git-ignored).

@@ -2,7 +2,7 @@
  * umcx_oracle.c - CPU oracle for the umcx photon-transport hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this
- * file's library, and only as the checker; the product (umcx_gb300/) never calls it and has no CPU fallback.
+ * file's library, and only to compute expected results; the product (umcx_gb300/) never calls it and has no CPU fallback.
  *
  * A plain-C restatement of the reference's photon loop (fangq/umcx, src/umcx.cpp), written to follow the
  * reference's floating-point expression order so that, single-threaded on x86-64 with -ffp-contract=off, its

@@ -94,7 +94,7 @@ std::string UserIO::help_text() const {
         "\t--dumpjson\tdump settings as json\n"
         "\t--dumpmask\tdump domain as binary json\n"
         "\t-h/--help\tprint help\n"
-        "\t-N/--net\tbrowse or download simulations from NeuroJSON.io (not available in this build)\n\n"
+        "\t-N/--net\tbrowse or download simulations from NeuroJSON.io (not available in this program)\n\n"
         "Built-in benchmarks: [\n";
     for (size_t i = 0; i < sizeof(kBenchmarks) / sizeof(kBenchmarks[0]); i++) {
         s += std::string("        \"") + kBenchmarks[i] + "\"";
@@ -132,7 +132,7 @@ UserIO::UserIO(int argc, const char* const argv[], bool device_domain) : domain_
             } else if ((arg == "-j" || arg == "--json") && i < argc) {
                 cfg.update(Value::parse(argv[i++]), true);
             } else if (arg == "-N" || arg == "--net") {
-                throw std::runtime_error("-N/--net needs network access, which this build does not provide");
+                throw std::runtime_error("-N/--net needs network access, which this program does not provide");
             } else if (arg[0] == '-' && i < argc) {
                 for (const FlagMap& f : kFlags) {
                     if (arg == f.shortf || arg == f.longf) {
@@ -463,7 +463,7 @@ static std::vector<unsigned char> inflate_bytes(const std::vector<unsigned char>
 #else
     (void)in;
     (void)gzip;
-    throw std::runtime_error("_ArrayZipData_ volumes need zlib, which this build was compiled without");
+    throw std::runtime_error("_ArrayZipData_ volumes need zlib, which this library was compiled without");
 #endif
 }
 
