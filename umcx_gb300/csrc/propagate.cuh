@@ -194,18 +194,36 @@ __device__ __forceinline__ void rotate(Photon& p, float stheta, float ctheta, fl
     if (vz > -1.f + FLT_EPSILON && vz < 1.f - FLT_EPSILON) {
         const float tmp0 = 1.f - vz * vz;
         const float tmp1 = STRICT ? stheta / sqrtf(tmp0) : stheta * rsqrtf(tmp0);
-        p.vx = tmp1 * (vx * vz * cphi - vy * sphi) + vx * ctheta;
-        p.vy = tmp1 * (vy * vz * cphi + vx * sphi) + vy * ctheta;
+        if constexpr (STRICT) {
+            p.vx = tmp1 * (vx * vz * cphi - vy * sphi) + vx * ctheta;
+            p.vy = tmp1 * (vy * vz * cphi + vx * sphi) + vy * ctheta;
+        } else {  // x and y as packed FP32x2 operations
+            const float2 vxy = make_float2(vx, vy);
+            const float vzc = vz * cphi;
+            const float2 a = __ffma2_rn(vxy, make_float2(vzc, vzc), __fmul2_rn(make_float2(-vy, vx), make_float2(sphi, sphi)));
+            const float2 r = __ffma2_rn(make_float2(tmp1, tmp1), a, __fmul2_rn(vxy, make_float2(ctheta, ctheta)));
+            p.vx = r.x;
+            p.vy = r.y;
+        }
         p.vz = -tmp1 * tmp0 * cphi + vz * ctheta;
     } else {
         p.vx = stheta * cphi;
         p.vy = stheta * sphi;
         p.vz = (vz > 0.f) ? ctheta : -ctheta;
     }
-    const float norm = rsqrt_<STRICT>(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
-    p.vx *= norm;
-    p.vy *= norm;
-    p.vz *= norm;
+    if constexpr (STRICT) {
+        const float norm = rsqrt_<STRICT>(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+        p.vx *= norm;
+        p.vy *= norm;
+        p.vz *= norm;
+    } else {
+        const float2 sq = __fmul2_rn(make_float2(p.vx, p.vy), make_float2(p.vx, p.vy));
+        const float norm = rsqrtf(sq.x + sq.y + p.vz * p.vz);
+        const float2 vxy = __fmul2_rn(make_float2(p.vx, p.vy), make_float2(norm, norm));
+        p.vx = vxy.x;
+        p.vy = vxy.y;
+        p.vz *= norm;
+    }
 }
 
 // MCX_photon::launch, L225-259; returns the launch weight
@@ -327,8 +345,11 @@ __device__ __forceinline__ bool skip_to_grid(const PV& P, Photon& p) {
 template <bool STRICT, class PV>
 __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, bool* crossed, float* moved) {
     const int bx = p.vx > 0.f, by = p.vy > 0.f, bz = p.vz > 0.f;
-    const float hx = fabsf((static_cast<float>(p.ix + bx) - p.px) * p.rx);
-    const float hy = fabsf((static_cast<float>(p.iy + by) - p.py) * p.ry);
+    // x and y as packed FP32x2 operations (each component rounded like the scalar operation)
+    const float2 hxy = __fmul2_rn(__fadd2_rn(make_float2(static_cast<float>(p.ix + bx), static_cast<float>(p.iy + by)),
+                                             make_float2(-p.px, -p.py)),
+                                  make_float2(p.rx, p.ry));
+    const float hx = fabsf(hxy.x), hy = fabsf(hxy.y);
     const float hz = fabsf((static_cast<float>(p.iz + bz) - p.pz) * p.rz);
     float dist = fminf(fminf(hx, hy), hz);
     p.flip = (dist == hx ? 0 : (dist == hy ? 1 : 2));
@@ -337,16 +358,18 @@ __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, boo
     *crossed = (used != p.lx);
     if constexpr (STRICT) {
         dist = (mus == 0.f) ? dist : (used / mus);
-        p.px = p.px + dist * p.vx;
-        p.py = p.py + dist * p.vy;
+        const float2 pxy = __fadd2_rn(make_float2(p.px, p.py), __fmul2_rn(make_float2(dist, dist), make_float2(p.vx, p.vy)));
+        p.px = pxy.x;
+        p.py = pxy.y;
         p.pz = p.pz + dist * p.vz;
         p.pw = p.pw * expf(-m.a.x * dist);
         p.lx -= used;
         p.ly += dist * m.a.w * kOneOverC0;
     } else {
         dist = (mus == 0.f) ? dist : (used * m.b.x);
-        p.px = p.px + dist * p.vx;
-        p.py = p.py + dist * p.vy;
+        const float2 pxy = __ffma2_rn(make_float2(dist, dist), make_float2(p.vx, p.vy), make_float2(p.px, p.py));
+        p.px = pxy.x;
+        p.py = pxy.y;
         p.pz = p.pz + dist * p.vz;
         p.pw = p.pw * __expf(-m.a.x * dist);
         p.lx -= used;
