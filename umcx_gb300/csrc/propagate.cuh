@@ -604,10 +604,10 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
         // `media` and stop the photon after kZeroStepLimit of them, like the step cap
         if (moved == 0.f) p.media += 0x10000u;
         else p.media &= 0xFFFFu;
-        if (++p.nsteps > P.step_cap || p.media >= (kZeroStepLimit << 16)) {
-            ev.term = true;
-            rare_count(kRareCap);
-        } else if (newvox != p.lastvox) {
+        const bool capped = ++p.nsteps > P.step_cap || p.media >= (kZeroStepLimit << 16);
+        if (capped) rare_count(kRareCap);
+        ev.term = capped;
+        if (!capped && newvox != p.lastvox) {
             c.cross++;
             ev.crossed = true;
             ev.left_vox = p.lastvox;
@@ -622,26 +622,26 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
                 p.lw = p.pw;
                 p.lz = 0.f;
             }
-            if (p.ly > P.tend) {
-                ev.term = true;
-            } else {
-                unsigned newmedia = (newvox >= 0) ? labels(newvox) : 0u;
-                const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
-                if (REFLECT && P.isreflect && m.a.w != n2) {
-                    rare_count(kRareRefl);
-                    if (reflect<STRICT>(p, m.a.w, n2)) {
-                        if (newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0) ev.term = true;
-                    } else {
-                        newvox = p.lastvox;
-                        newmedia = p.media;
-                    }
-                } else if (newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0)) {
-                    ev.term = true;
+            // past the last gate the photon ends here; otherwise the next voxel's label decides: leaving the grid
+            // or tissue -> background ends it, a refractive-index change reflects or transmits it (L291-306)
+            const bool late = p.ly > P.tend;
+            unsigned newmedia = (newvox >= 0 && !late) ? labels(newvox) : 0u;
+            const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
+            bool term = late || newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0);
+            if (REFLECT && P.isreflect && !late && m.a.w != n2) {
+                rare_count(kRareRefl);
+                if (reflect<STRICT>(p, m.a.w, n2)) {
+                    term = newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0;
+                } else {
+                    term = false;
+                    newvox = p.lastvox;
+                    newmedia = p.media;
                 }
-                if (!ev.term) {
-                    p.lastvox = newvox;
-                    p.media = newmedia;
-                }
+            }
+            ev.term = term;
+            if (!term) {
+                p.lastvox = newvox;
+                p.media = newmedia;
             }
         }
     }
