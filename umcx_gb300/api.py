@@ -361,9 +361,16 @@ class Batch:
         check(load().umcx_batch_run(self._h, C.byref(r)), self._ctx.handle, "umcx_batch_run")
         return r
 
-    def get(self, i: int):
+    def get(self, i: int, out=None):
+        """Simulation i's output volume [maxgate, nx, ny, nz] and tallies of the last run; out: an optional
+        caller-owned contiguous float32 array of at least that many elements, reused instead of a new one."""
         s = self.sims[i]
-        flu = np.zeros(s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3], np.float32) if s.issavevol else None
+        n = s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3]
+        flu = None
+        if s.issavevol:
+            flu = np.zeros(n, np.float32) if out is None else out.reshape(-1)[:n]
+            if flu.dtype != np.float32 or flu.size < n or not flu.flags.c_contiguous:
+                raise ValueError("out must be a contiguous float32 array of nx*ny*nz*maxgate elements")
         r = Result()
         check(load().umcx_batch_get(self._h, int(i), None if flu is None else flu.ctypes.data, C.byref(r)),
               self._ctx.handle, "umcx_batch_get")

@@ -973,8 +973,11 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                 }
             }
         }
-        if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane)) break;
+        // warp-uniform exits, tested every 16 iterations (a finished lane idles for at most 15 more)
+        if ((iter & 15u) == 0u) {
+            if (__all_sync(kFull, done)) break;
+            if (out_of_budget(B, iter, lane)) break;
+        }
 
         int dep_idx = -1;
         float dep_val = 0.f;
@@ -1102,8 +1105,11 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
                 if (!active) mismatch++;
             }
         }
-        if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane)) break;
+        // warp-uniform exits, tested every 16 iterations (a finished lane idles for at most 15 more)
+        if ((iter & 15u) == 0u) {
+            if (__all_sync(kFull, done)) break;
+            if (out_of_budget(B, iter, lane)) break;
+        }
         if (active) {
             Event ev;
             advance<false, REFLECT, true>(P, GlobalLabels{B.labels}, sm, p, ev, c);
@@ -1222,8 +1228,11 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 active = start_photon<false>(S, GlobalLabels{B.labels + S.label_off}, p, S.photon_offset + (g - begin[sim]));
             }
         }
-        if (__all_sync(kFull, done)) break;
-        if (out_of_budget(B, iter, lane)) break;
+        // warp-uniform exits, tested every 16 iterations (a finished lane idles for at most 15 more)
+        if ((iter & 15u) == 0u) {
+            if (__all_sync(kFull, done)) break;
+            if (out_of_budget(B, iter, lane)) break;
+        }
 
         long long dep_idx = -1;
         float dep_val = 0.f;
@@ -1232,11 +1241,11 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         if (active) {
             const SimDesc& S = sd[sim];
             advance<false, REFLECT, false>(S, GlobalLabels{B.labels + S.label_off}, sm + S.media_base, p, ev, c);
-            if (ev.crossed && S.issavevol && ev.gate >= 0) {
-                dep_idx = static_cast<long long>(S.out_off) + ev.left_vox +
-                          static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz);
-                dep_val = ev.dep_val;
-            }
+            const bool dep = ev.crossed && S.issavevol && ev.gate >= 0;
+            dep_idx = dep ? static_cast<long long>(S.out_off) + ev.left_vox +
+                                static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz)
+                          : -1;
+            dep_val = dep ? ev.dep_val : 0.f;
         }
         if (BP.aggregate) {
             const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
