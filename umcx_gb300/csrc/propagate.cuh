@@ -702,28 +702,6 @@ __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggreg
     if (dep_idx >= 0) deposit_add(B, dep_idx, dep_val);
 }
 
-// detected-photon append (L276-278, L429-435; MCX_detect::addphoton L164-176), called by all lanes (converged):
-// per detector a ballot, one atomic per warp, a prefix count for the slot.  Returns (through *slots) the slot
-// taken for each detector hit so callers can write extra per-record data.
-template <class WriteRecord>
-__device__ __forceinline__ void detect_converged(const KParams& P, const KBuffers& B, unsigned lane, bool tdet,
-                                                 const Photon& p, WriteRecord&& write) {
-    if (!__any_sync(kFull, tdet)) return;
-    for (int d = 0; d < P.detnum; d++) {
-        const bool hit = tdet && det_hit(P.det[d], p);
-        const unsigned hm = __ballot_sync(kFull, hit);
-        if (hm == 0u) continue;
-        const unsigned leader = __ffs(hm) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(&B.stats->detected, static_cast<unsigned long long>(__popc(hm)));
-        base = __shfl_sync(kFull, base, leader);
-        if (hit) {
-            const unsigned long long slot = base + __popc(hm & ((1u << lane) - 1u));
-            if (slot < P.maxdetphotons) write(d, slot);
-        }
-    }
-}
-
 // the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction]
 __device__ __forceinline__ void write_detp(const KParams& P, const KBuffers& B, const Photon& p, const float* ppath,
                                            unsigned stride, int d, unsigned long long slot) {
@@ -1023,23 +1001,29 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             }
         }
         deposit_converged(B, false, nullptr, tid, lane, dep_idx, dep_val);
-        const bool tdet = ev.term && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
-        detect_converged(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
-            if (B.detp) write_detp(P, B, p, ppath + tid, bd, d, slot);
-            DetRecord r;
-            r.photon = cur;
-            r.det = d + 1;
-            r.weight = p.pw;
-            r.time = p.ly;
-            r.pad = 0.f;
-            B.detrec[slot] = r;
-            float* ext = B.detext + slot * static_cast<unsigned long long>(2 * K);
-            for (int q = 0; q < K; q++) {
-                ext[q] = Lk[q * bd + tid];
-                ext[K + q] = Ck[q * bd + tid];
-            }
-        });
         if (ev.term) {
+            // detection (L429-435): the terminating lane appends its records, one atomic per detector hit, with
+            // the extended record (photon index, exit weight and time, per-label path and scatter counts)
+            if ((p.media & UMCX_LABEL_DET) && p.ly <= P.tend) {
+                for (int d = 0; d < P.detnum; d++) {
+                    if (!det_hit(P.det[d], p)) continue;
+                    const unsigned long long slot = atomicAdd(&B.stats->detected, 1ULL);
+                    if (slot >= P.maxdetphotons) continue;
+                    if (B.detp) write_detp(P, B, p, ppath + tid, bd, d, slot);
+                    DetRecord r;
+                    r.photon = cur;
+                    r.det = d + 1;
+                    r.weight = p.pw;
+                    r.time = p.ly;
+                    r.pad = 0.f;
+                    B.detrec[slot] = r;
+                    float* ext = B.detext + slot * static_cast<unsigned long long>(2 * K);
+                    for (int q = 0; q < K; q++) {
+                        ext[q] = Lk[q * bd + tid];
+                        ext[K + q] = Ck[q * bd + tid];
+                    }
+                }
+            }
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
                 tot += p.launchw;
                 esc += p.pw;
