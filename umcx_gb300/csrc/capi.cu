@@ -126,11 +126,11 @@ void validate(const umcx_sim* s) {
     if (s->srctype < 0 || s->srctype > 6) throw InputError("unknown source type");
 }
 
-Medium make_medium(const float* m) {
+Medium make_medium(const float* m, int outputtype) {
     Medium r;
     const float mua = m[0], mus = m[1], g = m[2], n = m[3];
     r.a = make_float4(mua, mus, g, n);
-    r.b = make_float4(mus != 0.f ? 1.f / mus : 0.f, mua != 0.f ? 1.f / mua : 0.f, g != 0.f ? 1.f / (2.f * g) : 0.f,
+    r.b = make_float4(mus != 0.f ? 1.f / mus : 0.f, deposit_factor(mua, outputtype), g != 0.f ? 1.f / (2.f * g) : 0.f,
                       n * kOneOverC0);
     r.c = make_float4(1.f - g * g, 1.f - g, 2.f * g, 1.f + g * g);
     return r;
@@ -242,7 +242,7 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     if (s->issavedet && s->maxdetphotons > 0 && !d_detp) throw InputError("detp is NULL but issavedet is set");
     KParams P = make_params(s, detpos);
     Medium hm[UMCX_MAX_MEDIA];
-    for (int i = 0; i < s->mediumnum; i++) hm[i] = make_medium(media + 4 * i);
+    for (int i = 0; i < s->mediumnum; i++) hm[i] = make_medium(media + 4 * i, s->outputtype);
 
     UMCX_CK(ctx->media.ensure(sizeof(Medium) * UMCX_MAX_MEDIA));
     UMCX_CK(ctx->stats.ensure(sizeof(KStats)));
@@ -498,7 +498,7 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         KParams P = make_params(s, detpos);
         P.maxdetphotons = static_cast<unsigned>(cap);
         Medium hm[UMCX_MAX_MEDIA];
-        for (int i = 0; i < K; i++) hm[i] = make_medium(media + 4 * i);
+        for (int i = 0; i < K; i++) hm[i] = make_medium(media + 4 * i, s->outputtype);
         UMCX_CK(cudaMemcpyAsync(ctx->media.ptr, hm, sizeof(Medium) * K, cudaMemcpyHostToDevice, st));
         UMCX_CK(cudaMemsetAsync(ctx->stats.ptr, 0, sizeof(KStats), st));
         UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), st));
@@ -976,7 +976,7 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
             b->out_off[static_cast<size_t>(i)] = b->nout_total;
             b->nout_total += s->issavevol ? nvox * s->dim[3] : 0;
             media_first[static_cast<size_t>(i)] = table.size();
-            for (int m = 0; m < s->mediumnum; m++) table.push_back(make_medium(media[i] + 4 * m));
+            for (int m = 0; m < s->mediumnum; m++) table.push_back(make_medium(media[i] + 4 * m, s->outputtype));
             if (s->isreflect) b->reflect = true;
             if (s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM)) b->fp64 = true;
         }

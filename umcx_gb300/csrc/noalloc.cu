@@ -133,7 +133,7 @@ extern "C" int umcx_gpu_forward_noalloc(int device, const umcx_sim* s, const uin
     for (int i = 0; i < s->mediumnum; i++) {
         const float mua = media[4 * i], mus = media[4 * i + 1], g = media[4 * i + 2], n = media[4 * i + 3];
         hm[i].a = make_float4(mua, mus, g, n);
-        hm[i].b = make_float4(mus != 0.f ? 1.f / mus : 0.f, mua != 0.f ? 1.f / mua : 0.f,
+        hm[i].b = make_float4(mus != 0.f ? 1.f / mus : 0.f, deposit_factor(mua, s->outputtype),
                               g != 0.f ? 1.f / (2.f * g) : 0.f, n * kOneOverC0);
         hm[i].c = make_float4(1.f - g * g, 1.f - g, 2.f * g, 1.f + g * g);
     }

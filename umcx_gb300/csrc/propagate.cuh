@@ -43,11 +43,18 @@ constexpr unsigned kDefaultStepCap = 1u << 24;  // steps of one photon before it
 
 enum Kind : int { kForward = 0, kAdjoint = 1, kReplay = 2 };
 
-// per-label optical constants (48 bytes): a = {mua, mus, g, n}; b = {1/mus (0 if mus = 0), 1/mua (0 if mua = 0),
+// per-label optical constants (48 bytes): a = {mua, mus, g, n}; b = {1/mus (0 if mus = 0), deposit factor,
 // 1/(2g), n / c0}; c = {1 - g^2, 1 - g, 2g, 1 + g^2}
 struct Medium {
     float4 a, b, c;
 };
+
+// Factor of MCX_photon::save's deposit (L359-363) for an output type: the weight loss itself for energy output,
+// divided by mua for fluence and fluence rate, and -1 (deposit weight x path length instead) when mua < FLT_EPSILON
+__host__ __device__ inline float deposit_factor(float mua, int outputtype) {
+    if (outputtype == UMCX_OUT_ENERGY) return 1.f;
+    return mua < FLT_EPSILON ? -1.f : 1.f / mua;
+}
 
 struct KStats {
     double escape;
@@ -485,13 +492,18 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
-// deposit value of MCX_photon::save (L359-363)
+// deposit value of MCX_photon::save (L359-363).  The fast path reads the output type and the mua < FLT_EPSILON case
+// from the medium's deposit factor (Medium.b.y, see deposit_factor); the strict path evaluates them like the reference.
 template <bool STRICT, class PV>
 __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, const Medium& m) {
-    if (P.outputtype == UMCX_OUT_ENERGY) return p.lw - p.pw;
-    if (m.a.x < FLT_EPSILON) return p.lw * p.lz;
-    if constexpr (STRICT) return (p.lw - p.pw) / m.a.x;
-    else return (p.lw - p.pw) * m.b.y;
+    if constexpr (STRICT) {
+        if (P.outputtype == UMCX_OUT_ENERGY) return p.lw - p.pw;
+        if (m.a.x < FLT_EPSILON) return p.lw * p.lz;
+        return (p.lw - p.pw) / m.a.x;
+    } else {
+        const float f = m.b.y;
+        return f < 0.f ? p.lw * p.lz : (p.lw - p.pw) * f;
+    }
 }
 
 // one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
@@ -565,6 +577,12 @@ struct PackedLabels {
     }
 };
 
+// Boundary reflection switch of one simulation.  A single-simulation kernel is instantiated with REFLECT equal to
+// its isreflect, so nothing is read at run time; a batch kernel with reflections reads each simulation's flag.
+__device__ __forceinline__ bool reflect_on(const KParams&) { return true; }
+template <class PV>
+__device__ __forceinline__ bool reflect_on(const PV& S) { return S.isreflect != 0; }
+
 // L761-762 + L262-271: seed photon idx, launch it, move it onto the grid; false when it misses the grid
 template <bool STRICT, class PV, class LV>
 __device__ __forceinline__ bool start_photon(const PV& P, const LV& labels, Photon& p, unsigned long long idx) {
@@ -628,7 +646,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
             unsigned newmedia = (newvox >= 0 && !late) ? labels(newvox) : 0u;
             const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
             bool term = late || newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0);
-            if (REFLECT && P.isreflect && !late && m.a.w != n2) {
+            if (REFLECT && reflect_on(P) && !late && m.a.w != n2) {
                 rare_count(kRareRefl);
                 if (reflect<STRICT>(p, m.a.w, n2)) {
                     term = newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0;
