@@ -39,6 +39,7 @@ constexpr float kOneOverC0 = 3.335640951981520e-12f;  // L29
 constexpr float kPi = 3.1415926535897932385f;         // L30
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned kZeroStepLimit = 255;  // consecutive zero-length steps before a photon is stopped
+constexpr unsigned kStoppedBit = 0x8000u;  // Photon::media bit 15: the photon was stopped by the step cap or guard
 constexpr unsigned kDefaultStepCap = 1u << 24;  // steps of one photon before it is stopped
 
 enum Kind : int { kForward = 0, kAdjoint = 1, kReplay = 2 };
@@ -577,6 +578,11 @@ struct PackedLabels {
     }
 };
 
+// the kernels call this where a photon ends: photons stopped by the step cap or the zero-progress guard
+__device__ __forceinline__ void count_stopped(const Photon& p) {
+    if (p.media & kStoppedBit) rare_count(kRareCap);
+}
+
 // Boundary reflection switch of one simulation.  A single-simulation kernel is instantiated with REFLECT equal to
 // its isreflect, so nothing is read at run time; a batch kernel with reflections reads each simulation's flag.
 __device__ __forceinline__ bool reflect_on(const KParams&) { return true; }
@@ -623,7 +629,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
         if (moved == 0.f) p.media += 0x10000u;
         else p.media &= 0xFFFFu;
         const bool capped = ++p.nsteps > P.step_cap || p.media >= (kZeroStepLimit << 16);
-        if (capped) rare_count(kRareCap);
+        p.media |= capped ? kStoppedBit : 0u;  // counted where the photon ends (count_stopped)
         ev.term = capped;
         if (!capped && newvox != p.lastvox) {
             c.cross++;
@@ -877,6 +883,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
         }
         deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
         if (ev.term) {
+            count_stopped(p);
             // detection (L276-278, L429-435): a few photons per thousand, so each lane appends its own records
             // with one atomic per hit instead of a per-iteration warp vote
             if (SAVEDET && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend) {
@@ -1020,6 +1027,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
         }
         deposit_converged(B, false, nullptr, tid, lane, dep_idx, dep_val);
         if (ev.term) {
+            count_stopped(p);
             // detection (L429-435): the terminating lane appends its records, one atomic per detector hit, with
             // the extended record (photon index, exit weight and time, per-label path and scatter counts)
             if ((p.media & UMCX_LABEL_DET) && p.ly <= P.tend) {
@@ -1119,6 +1127,7 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
                 atomicAdd(B.jacobian + static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox,
                           -rec.weight * ev.seg);
             if (ev.term) {
+                count_stopped(p);
                 const bool same = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend && det_hit(P.det[rec.det - 1], p) &&
                                   p.pw == rec.weight;
                 if (!same) mismatch++;
@@ -1269,6 +1278,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
             deposit_add64(B, dep_idx, dep_val);
         }
         if (ev.term) {
+            count_stopped(p);
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
                 tot += p.launchw;
                 esc += p.pw;
