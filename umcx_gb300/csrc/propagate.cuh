@@ -427,61 +427,88 @@ __device__ __forceinline__ void scatter(Photon& p, const Medium& m) {
     p.rz = rcp_<STRICT>(p.vz);
 }
 
+template <bool STRICT>
+__device__ __forceinline__ float div_(float a, float b) {
+    if constexpr (STRICT) return a / b;
+    else return __fdividef(a, b);
+}
+
+// square root of a positive argument
+template <bool STRICT>
+__device__ __forceinline__ float sqrt_pos_(float x) {
+    if constexpr (STRICT) return sqrtf(x);
+    else return x * rsqrtf(x);
+}
+
+// C99 nextafterf for finite arguments, from its definition: y itself when x == y, else the representable float next
+// to x in the direction of y (one unit in the last place; the smallest subnormal, signed like y, from zero)
+__device__ __forceinline__ float next_toward(float x, float y) {
+    if (x == y) return y;
+    if (x == 0.f) return __int_as_float((__float_as_int(y) & static_cast<int>(0x80000000u)) | 1);
+    return __int_as_float(__float_as_int(x) + (((x < y) == (x > 0.f)) ? 1 : -1));
+}
+
+template <bool STRICT>
+__device__ __forceinline__ float nextafter_(float x, float y) {
+    if constexpr (STRICT) return nextafterf(x, y);
+    else return next_toward(x, y);
+}
+
 // reflectcoeff + reflect + transmit, L381-417; returns true when the photon is transmitted.  On reflection the
-// photon is put back just inside the current voxel and the caller keeps (lastvox, media).
+// photon is put back just inside the current voxel and the caller keeps (lastvox, media).  The crossed axis (flip)
+// is selected arithmetically rather than by branches: this block runs in about a third of the warp iterations
+// (2 % of crossings reflect, but any lane of the warp brings the whole warp through it).
 template <bool STRICT>
 __device__ __forceinline__ bool reflect(Photon& p, float n1, float n2) {
-    const float icos = fabsf((p.flip == 0) ? p.vx : (p.flip == 1 ? p.vy : p.vz));
+    const int f = p.flip;
+    const float icos = fabsf((f == 0) ? p.vx : (f == 1 ? p.vy : p.vz));
     const float tmp0 = n1 * n1, tmp1 = n2 * n2;
-    float tmp2 = 1.f - tmp0 / tmp1 * (1.f - icos * icos);
+    float tmp2 = 1.f - div_<STRICT>(tmp0, tmp1) * (1.f - icos * icos);
     float rtotal = 1.f;
     if (tmp2 > 0.f) {
         float re = tmp0 * icos * icos + tmp1 * tmp2;
-        tmp2 = sqrtf(tmp2);
+        tmp2 = sqrt_pos_<STRICT>(tmp2);
         const float im = 2.f * n1 * n2 * icos * tmp2;
-        const float rp = (re - im) / (re + im);
+        const float rp = div_<STRICT>(re - im, re + im);
         re = tmp1 * icos * icos + tmp0 * tmp2 * tmp2;
-        rtotal = (rp + (re - im) / (re + im)) * 0.5f;
+        rtotal = (rp + div_<STRICT>(re - im, re + im)) * 0.5f;
     }
     if (rtotal < 1.f && rng_rand01(p.rng) > rtotal) {  // transmit (L396-404)
-        const float k = n1 / n2;
+        const float k = div_<STRICT>(n1, n2);
         p.vx *= k;
         p.vy *= k;
         p.vz *= k;
         const float sq = p.vx * p.vx + p.vy * p.vy + p.vz * p.vz;
-        if (p.flip == 0) {
-            const float t = sq - p.vx * p.vx;
-            p.vx = (t < 1.f) ? sqrtf(1.f - t) * sgnf(p.vx) : 0.f;
-        } else if (p.flip == 1) {
-            const float t = sq - p.vy * p.vy;
-            p.vy = (t < 1.f) ? sqrtf(1.f - t) * sgnf(p.vy) : 0.f;
-        } else {
-            const float t = sq - p.vz * p.vz;
-            p.vz = (t < 1.f) ? sqrtf(1.f - t) * sgnf(p.vz) : 0.f;
-        }
+        const float vc = (f == 0) ? p.vx : (f == 1 ? p.vy : p.vz);
+        const float t = sq - vc * vc;
+        const float nv = (t < 1.f) ? sqrt_pos_<STRICT>(1.f - t) * sgnf(vc) : 0.f;
+        p.vx = (f == 0) ? nv : p.vx;
+        p.vy = (f == 1) ? nv : p.vy;
+        p.vz = (f == 2) ? nv : p.vz;
         const float norm = rsqrt_<STRICT>(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
         p.vx *= norm;
         p.vy *= norm;
         p.vz *= norm;
         return true;  // the inverse direction is deliberately left as it was (as in the reference)
     }
-    // REFLECT_PHOTON (L31)
-    if (p.flip == 0) {
-        p.vx = -p.vx;
-        p.rx = -p.rx;
-        p.px = nextafterf(static_cast<float>(static_cast<int>(p.px + 0.5f)), sgnf(p.vx));
-        p.ix = static_cast<int>(p.px);
-    } else if (p.flip == 1) {
-        p.vy = -p.vy;
-        p.ry = -p.ry;
-        p.py = nextafterf(static_cast<float>(static_cast<int>(p.py + 0.5f)), sgnf(p.vy));
-        p.iy = static_cast<int>(p.py);
-    } else {
-        p.vz = -p.vz;
-        p.rz = -p.rz;
-        p.pz = nextafterf(static_cast<float>(static_cast<int>(p.pz + 0.5f)), sgnf(p.vz));
-        p.iz = static_cast<int>(p.pz);
-    }
+    // REFLECT_PHOTON (L31): the crossed axis' direction and inverse direction change sign, the position snaps to the
+    // nearest voxel face and moves one float towards the new direction
+    const float vc = -((f == 0) ? p.vx : (f == 1 ? p.vy : p.vz));
+    const float pc = (f == 0) ? p.px : (f == 1 ? p.py : p.pz);
+    const float np = nextafter_<STRICT>(static_cast<float>(static_cast<int>(pc + 0.5f)), sgnf(vc));
+    const int ni = static_cast<int>(np);
+    p.vx = (f == 0) ? vc : p.vx;
+    p.vy = (f == 1) ? vc : p.vy;
+    p.vz = (f == 2) ? vc : p.vz;
+    p.rx = (f == 0) ? -p.rx : p.rx;
+    p.ry = (f == 1) ? -p.ry : p.ry;
+    p.rz = (f == 2) ? -p.rz : p.rz;
+    p.px = (f == 0) ? np : p.px;
+    p.py = (f == 1) ? np : p.py;
+    p.pz = (f == 2) ? np : p.pz;
+    p.ix = (f == 0) ? ni : p.ix;
+    p.iy = (f == 1) ? ni : p.iy;
+    p.iz = (f == 2) ? ni : p.iz;
     return false;
 }
 
