@@ -638,11 +638,11 @@ __device__ __forceinline__ bool start_photon(const PV& P, const LV& labels, Phot
 // volume is saved (per-voxel path lengths for the adjoint and the replay); trajectories do not depend on it.
 template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV, class LV>
 __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Medium* sm, Photon& p, Event& ev,
-                                        Counters& c) {
+                                        Counters& c, bool active = true) {
     ev.crossed = false;
     ev.term = false;
     ev.scattered = false;
-    if (p.lx > 0.f) {
+    if (active && p.lx > 0.f) {
         const unsigned mid = p.media & UMCX_LABEL_MASK;
         const Medium m = sm[mid];
         bool crossed;
@@ -696,7 +696,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
             }
         }
     }
-    if (!ev.term && p.lx <= 0.f) {
+    if (active && !ev.term && p.lx <= 0.f) {
         ev.scattered = true;
         ev.scat_mid = p.media & UMCX_LABEL_MASK;
         scatter<STRICT>(p, sm[ev.scat_mid]);
@@ -896,18 +896,13 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
             if (out_of_budget(B, iter, lane)) break;
         }
 
-        int dep_idx = -1;
-        float dep_val = 0.f;
         Event ev;
-        ev.term = false;
-        if (active) {
-            advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c);
-            if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0)
-                ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
-            const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
-            dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
-            dep_val = dep ? ev.dep_val : 0.f;
-        }
+        advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c, active);  // no event on an idle lane
+        if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0)
+            ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
+        const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
+        const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
+        const float dep_val = dep ? ev.dep_val : 0.f;
         deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
         if (ev.term) {
             count_stopped(p);
