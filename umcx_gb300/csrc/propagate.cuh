@@ -32,6 +32,7 @@
 #include <cstdint>
 
 #include "../../include/umcx_gpu.h"
+#include "next_toward.h"
 
 namespace umcx_dev {
 
@@ -438,14 +439,6 @@ template <bool STRICT>
 __device__ __forceinline__ float sqrt_pos_(float x) {
     if constexpr (STRICT) return sqrtf(x);
     else return x * rsqrtf(x);
-}
-
-// C99 nextafterf for finite arguments, from its definition: y itself when x == y, else the representable float next
-// to x in the direction of y (one unit in the last place; the smallest subnormal, signed like y, from zero)
-__device__ __forceinline__ float next_toward(float x, float y) {
-    if (x == y) return y;
-    if (x == 0.f) return __int_as_float((__float_as_int(y) & static_cast<int>(0x80000000u)) | 1);
-    return __int_as_float(__float_as_int(x) + (((x < y) == (x > 0.f)) ? 1 : -1));
 }
 
 template <bool STRICT>
