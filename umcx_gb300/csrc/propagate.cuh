@@ -17,7 +17,8 @@
 //  * the per-label optical table (with reciprocals and Henyey-Greenstein constants precomputed) sits in shared
 //    memory; labels are uint8 loaded through the read-only path;
 //  * fluence deposits are issued after the divergent part of the iteration, optionally aggregated per warp with
-//    __match_any_sync on the output index; detected photons are appended with a ballot + prefix count per detector;
+//    __match_any_sync on the output index; detected photons are appended, by the lanes that end a photon, with a
+//    ballot + prefix count per detector and one atomic per warp;
 //  * energy tallies accumulate in FP64 per lane and reach global memory once per warp at exit;
 //  * every loop is bounded: a per-photon step cap and a wall-clock deadline (%globaltimer) end the kernel with an
 //    error flag instead of hanging.
@@ -746,6 +747,31 @@ __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggreg
     if (dep_idx >= 0) deposit_add(B, dep_idx, dep_val);
 }
 
+// Detected-photon append (L276-278, L429-435; MCX_detect::addphoton L164-176), called only by the lanes of a warp
+// that end a photon in this iteration (no vote runs in the other iterations).  Among those lanes, per detector: a
+// ballot of the hits, one atomic per warp for the block of slots, and each hit's slot from a prefix count of the
+// ballot.  write(d, slot) stores the record of a slot below the buffer size; all hits are counted.
+template <class WriteRecord>
+__device__ __forceinline__ void append_detected(const KParams& P, const KBuffers& B, unsigned lane, bool tdet,
+                                                const Photon& p, WriteRecord&& write) {
+    const unsigned group = __activemask();
+    if (!__any_sync(group, tdet)) return;
+    const unsigned below = (1u << lane) - 1u;
+    for (int d = 0; d < P.detnum; d++) {
+        const bool hit = tdet && det_hit(P.det[d], p);
+        const unsigned hm = __ballot_sync(group, hit);
+        if (hm == 0u) continue;
+        const unsigned leader = __ffs(hm) - 1u;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&B.stats->detected, static_cast<unsigned long long>(__popc(hm)));
+        base = __shfl_sync(group, base, leader);
+        if (hit) {
+            const unsigned long long slot = base + __popc(hm & below);
+            if (slot < P.maxdetphotons) write(d, slot);
+        }
+    }
+}
+
 // the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction]
 __device__ __forceinline__ void write_detp(const KParams& P, const KBuffers& B, const Photon& p, const float* ppath,
                                            unsigned stride, int d, unsigned long long slot) {
@@ -899,14 +925,11 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
         deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
         if (ev.term) {
             count_stopped(p);
-            // detection (L276-278, L429-435): a few photons per thousand, so each lane appends its own records
-            // with one atomic per hit instead of a per-iteration warp vote
-            if (SAVEDET && (p.media & UMCX_LABEL_DET) && p.ly <= P.tend) {
-                for (int d = 0; d < P.detnum; d++) {
-                    if (!det_hit(P.det[d], p)) continue;
-                    const unsigned long long slot = atomicAdd(&B.stats->detected, 1ULL);
-                    if (slot < P.maxdetphotons) write_detp(P, B, p, ppath + tid, blockDim.x, d, slot);
-                }
+            if (SAVEDET) {
+                const bool tdet = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
+                append_detected(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
+                    write_detp(P, B, p, ppath + tid, blockDim.x, d, slot);
+                });
             }
             if ((p.media & UMCX_LABEL_MASK) != 0u) {  // energy tallies (L765-770)
                 tally[tid] += static_cast<double>(lwbuf[tid]);
@@ -1045,26 +1068,22 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             count_stopped(p);
             // detection (L429-435): the terminating lane appends its records, one atomic per detector hit, with
             // the extended record (photon index, exit weight and time, per-label path and scatter counts)
-            if ((p.media & UMCX_LABEL_DET) && p.ly <= P.tend) {
-                for (int d = 0; d < P.detnum; d++) {
-                    if (!det_hit(P.det[d], p)) continue;
-                    const unsigned long long slot = atomicAdd(&B.stats->detected, 1ULL);
-                    if (slot >= P.maxdetphotons) continue;
-                    if (B.detp) write_detp(P, B, p, ppath + tid, bd, d, slot);
-                    DetRecord r;
-                    r.photon = cur;
-                    r.det = d + 1;
-                    r.weight = p.pw;
-                    r.time = p.ly;
-                    r.pad = 0.f;
-                    B.detrec[slot] = r;
-                    float* ext = B.detext + slot * static_cast<unsigned long long>(2 * K);
-                    for (int q = 0; q < K; q++) {
-                        ext[q] = Lk[q * bd + tid];
-                        ext[K + q] = Ck[q * bd + tid];
-                    }
+            const bool tdet = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
+            append_detected(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
+                if (B.detp) write_detp(P, B, p, ppath + tid, bd, d, slot);
+                DetRecord r;
+                r.photon = cur;
+                r.det = d + 1;
+                r.weight = p.pw;
+                r.time = p.ly;
+                r.pad = 0.f;
+                B.detrec[slot] = r;
+                float* ext = B.detext + slot * static_cast<unsigned long long>(2 * K);
+                for (int q = 0; q < K; q++) {
+                    ext[q] = Lk[q * bd + tid];
+                    ext[K + q] = Ck[q * bd + tid];
                 }
-            }
+            });
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
                 tot += p.launchw;
                 esc += p.pw;
