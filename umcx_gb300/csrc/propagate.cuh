@@ -26,7 +26,8 @@
 // STRICT = true evaluates every expression like the reference (IEEE division, expf/logf/sinf/cosf/acosf; the
 // translation unit is compiled without FMA contraction).  STRICT = false ("fast", the production path) uses the
 // hardware approximations __expf/__logf/__sincosf, reciprocal multiplies, and sin(theta) = sqrt(1 - cos^2) instead
-// of sincos(acos(cos)): the same distributions, different last bits.
+// of sincos(acos(cos)), and its translation units are compiled with --use_fast_math (single-precision denormals
+// flushed to zero): the same distributions, different last bits.
 #pragma once
 
 #include <cfloat>
