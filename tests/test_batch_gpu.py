@@ -97,3 +97,22 @@ def test_autotuners(ctx):
     ctx.set_tuning()
     bb = autotune_batch(ctx, small_batch(4, scale=0.01), fraction=1.0, candidates=((256, 1), (512, 2)))
     assert bb["block_size"] in (256, 512)
+
+
+def test_batch_outputs_into_caller_buffer(ctx):
+    from umcx_gb300.api import Batch
+
+    jobs = small_batch(4, scale=0.01)
+    b = Batch.from_jobs(ctx, jobs)
+    b.run()
+    biggest = max(j.sim.dim[0] * j.sim.dim[1] * j.sim.dim[2] * j.sim.dim[3] for j in jobs)
+    out = np.full(biggest, -1.0, np.float32)
+    for i in range(len(jobs)):
+        ref, r_ref = b.get(i)
+        got, r_got = b.get(i, out=out)
+        assert got.base is not None and np.shares_memory(got, out)
+        np.testing.assert_array_equal(got, ref)
+        assert r_got.energy_total == r_ref.energy_total
+    with pytest.raises(ValueError):
+        b.get(0, out=np.zeros(10, np.float32))
+    b.close()

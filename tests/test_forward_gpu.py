@@ -258,3 +258,20 @@ def test_mcx_run_json_entry(tmp_path, monkeypatch):
     assert load().MCX_run_json(json.dumps(cfg).encode()) == 0
     assert (tmp_path / "rj.bnii").exists() and (tmp_path / "rj_detp.jdb").exists()
     assert load().MCX_run_json(b'{"Session":{}}') != 0
+
+
+def test_caller_owned_output_arrays(ctx):
+    """Context.forward writes into output arrays the caller reuses from call to call (stale contents overwritten)."""
+    job = job_for(C2, 20000)
+    s = job.sim
+    ref = ctx.forward(s, job.labels, job.media, job.detpos)
+    nout = s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3]
+    flu = np.full(nout, 7.0, np.float32)
+    dp = np.full(s.maxdetphotons * ref.detp.shape[1], 7.0, np.float32)
+    for _ in range(2):
+        out = ctx.forward(s, job.labels, job.media, job.detpos, fluence=flu, detp=dp)
+        assert np.shares_memory(out.fluence, flu)
+        assert out.result.steps == ref.result.steps and out.result.detected == ref.result.detected
+        np.testing.assert_allclose(out.fluence, ref.fluence, rtol=1e-5, atol=1e-7)
+    with pytest.raises(ValueError):
+        ctx.forward(s, job.labels, job.media, job.detpos, fluence=np.zeros(10, np.float32))
