@@ -135,6 +135,7 @@ class Job:
 
 
 def detp_columns(sim: Sim) -> int:
+    """Floats per detected-photon row for sim's SaveDetFlag (umcx_detp_columns, the reference's L157)."""
     return load().umcx_detp_columns(C.byref(sim))
 
 
@@ -147,6 +148,7 @@ def measure_peaks(device: int = 0) -> dict:
 
 
 def seeds_from_rngseed(seed: int) -> np.ndarray:
+    """The four session seeds the reference derives from RNGSeed (srand + four rand() calls, L724-727)."""
     out = (C.c_uint32 * 4)()
     check(load().umcx_seeds_from_rngseed(int(seed), out), None, "umcx_seeds_from_rngseed")
     return np.array(list(out), np.uint32)
@@ -154,6 +156,9 @@ def seeds_from_rngseed(seed: int) -> np.ndarray:
 
 @dataclass
 class Forward:
+    """Outputs of one forward simulation: fluence [maxgate, nx, ny, nz] (not normalised), detected-photon rows
+    [saved, columns] and the tallies (energies, event counts, kernel time)."""
+
     fluence: np.ndarray | None
     detp: np.ndarray | None
     result: Result
@@ -312,6 +317,7 @@ class Context:
                 "label_pack": best.label_pack, "probe_ms": ms.value}
 
     def rng_dump(self, seeds, photon_offset: int, nphoton: int, ndraw: int) -> np.ndarray:
+        """rand01() draws [nphoton, ndraw] of photons photon_offset.. computed on the device (known-answer hook)."""
         s = (C.c_uint32 * 4)(*[int(x) for x in seeds])
         out = np.zeros(nphoton * ndraw, np.float32)
         check(load().umcx_gpu_rng_dump(self._h, s, int(photon_offset), int(nphoton), int(ndraw), out.ctypes.data),
@@ -357,6 +363,7 @@ class Batch:
         return int(p)
 
     def run(self) -> Result:
+        """Run the whole batch once (graph launch); returns the summed tallies and the graph's device time."""
         r = Result()
         check(load().umcx_batch_run(self._h, C.byref(r)), self._ctx.handle, "umcx_batch_run")
         return r
