@@ -956,7 +956,8 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
 //               = (cnt_k S - R_k)/mus_k - (L_k S - Q_k + T_k)   with R_k += S at each scatter, T_k += F_j l_j
 // so each deposit and each scatter updates one label's tallies (O(1) per event).
 //
-// Shared memory: double ga[K][bd], gs[K][bd] | Medium[K] | float ppath[ppathlen][bd] | float L, cnt, Q, T, E, R[K][bd]
+// Shared memory: double ga[K][bd], gs[K][bd] | Medium[K] | float ppath[ppathlen][bd] | float L, cnt, Q, T, E, R[K][bd] |
+// double total, escape[bd] | u64 photon index[bd]
 template <bool REFLECT>
 __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffers B) {
     extern __shared__ double smem8[];
@@ -972,6 +973,9 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     float* Tk = Qk + K * bd;
     float* Ek = Tk + K * bd;
     float* Rk = Ek + K * bd;
+    // touched once per photon, so kept out of the loop's registers: FP64 energy tallies and the photon index
+    double* etally = reinterpret_cast<double*>(Rk + K * bd);                    // [2][bd]: total, escape
+    unsigned long long* cur = reinterpret_cast<unsigned long long*>(etally + 2 * bd);  // [bd]
     load_media(P, B.media, sm);
 
     const unsigned tid = threadIdx.x;
@@ -987,10 +991,11 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     p.media = 0;
     p.lastvox = -1;
     bool active = false, done = false;
-    double tot = 0.0, esc = 0.0;
+    etally[tid] = 0.0;
+    etally[bd + tid] = 0.0;
+    cur[tid] = 0;
     Counters c;
     float S = 0.f;
-    unsigned long long cur = 0;
 
     for (unsigned iter = 0;; iter++) {
         if (!active && !done) {
@@ -999,8 +1004,8 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                 done = true;
             } else {
                 rare_count(kRareLaunch);
-                cur = P.photon_offset + k;
-                active = start_photon<false>(P, GlobalLabels{B.labels}, p, cur);
+                cur[tid] = P.photon_offset + k;
+                active = start_photon<false>(P, GlobalLabels{B.labels}, p, P.photon_offset + k);
                 if (active) {
                     S = 0.f;
                     for (int q = 0; q < P.ppathlen; q++) ppath[q * bd + tid] = 0.f;
@@ -1073,7 +1078,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             append_detected(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
                 if (B.detp) write_detp(P, B, p, ppath + tid, bd, d, slot);
                 DetRecord r;
-                r.photon = cur;
+                r.photon = cur[tid];
                 r.det = d + 1;
                 r.weight = p.pw;
                 r.time = p.ly;
@@ -1086,8 +1091,8 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                 }
             });
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
-                tot += p.launchw;
-                esc += p.pw;
+                etally[tid] += static_cast<double>(p.launchw);
+                etally[bd + tid] += static_cast<double>(p.pw);
             }
             for (int q = 0; q < K; q++) {
                 const float L = Lk[q * bd + tid];
@@ -1100,7 +1105,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             active = false;
         }
     }
-    flush_tallies(B, lane, tot, esc, c);
+    flush_tallies(B, lane, etally[tid], etally[bd + tid], c);
     rare_flush(B);
     // per-label gradient accumulators: warp reduction in FP64, one atomic per warp and label
     for (int q = 0; q < K; q++) {
