@@ -5,7 +5,8 @@ namespace umcx_dev {
 
 size_t batch_smem(int nsim, int total_media, int block) {
     return sizeof(SimDesc) * static_cast<size_t>(nsim) + sizeof(unsigned long long) * static_cast<size_t>((nsim + 2) & ~1) +
-           sizeof(Medium) * static_cast<size_t>(total_media) + sizeof(float) * static_cast<size_t>(block);
+           sizeof(Medium) * static_cast<size_t>(total_media) + sizeof(float) * static_cast<size_t>(block) +
+           2 * sizeof(double) * static_cast<size_t>(block);  // + per-lane energy tallies
 }
 
 cudaError_t configure_batch_kernels() {

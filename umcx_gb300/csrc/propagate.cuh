@@ -1218,7 +1218,8 @@ __device__ __forceinline__ void deposit_add64(const KBuffers& B, long long idx, 
 // search over the prefix sums names the simulation, whose descriptor and optical table sit in shared memory.
 // Consecutive indices belong to the same simulation, so at any moment only one or two simulations are in flight and
 // their outputs stay in L2, while the tail of one simulation overlaps the start of the next.
-// Shared memory: SimDesc[nsim] | u64 begin[nsim + 1] (padded to 16 B) | Medium[total_media] | float aggbuf[blockDim]
+// Shared memory: SimDesc[nsim] | u64 begin[nsim + 1] (padded to 16 B) | Medium[total_media] | float aggbuf[blockDim] |
+// double escape, total[blockDim]
 template <bool REFLECT>
 __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers B) {
     extern __shared__ float4 smem4[];
@@ -1226,6 +1227,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
     unsigned long long* begin = reinterpret_cast<unsigned long long*>(sd + BP.nsim);
     Medium* sm = reinterpret_cast<Medium*>(begin + ((BP.nsim + 2) & ~1));
     float* aggbuf = reinterpret_cast<float*>(sm + BP.total_media);
+    double* etally = reinterpret_cast<double*>(aggbuf + blockDim.x);  // [2][blockDim]: escape, total of `tally_sim`
     {
         const float4* s = reinterpret_cast<const float4*>(BP.sims);
         float4* d = reinterpret_cast<float4*>(sd);
@@ -1249,7 +1251,8 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
     p.lastvox = -1;
     bool active = false, done = false;
     int sim = 0, tally_sim = -1;
-    double tot = 0.0, esc = 0.0;
+    etally[tid] = 0.0;  // per-lane FP64 tallies of the current simulation, in shared memory
+    etally[blockDim.x + tid] = 0.0;
     Counters c;
 
     for (unsigned iter = 0;; iter++) {
@@ -1266,13 +1269,13 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 }
                 sim = lo;
                 if (sim != tally_sim) {
-                    if (tally_sim >= 0 && (tot != 0.0 || esc != 0.0)) {
-                        atomicAdd(BP.tallies + 2 * tally_sim, esc);
-                        atomicAdd(BP.tallies + 2 * tally_sim + 1, tot);
+                    if (tally_sim >= 0 && (etally[blockDim.x + tid] != 0.0 || etally[tid] != 0.0)) {
+                        atomicAdd(BP.tallies + 2 * tally_sim, etally[tid]);
+                        atomicAdd(BP.tallies + 2 * tally_sim + 1, etally[blockDim.x + tid]);
                     }
                     tally_sim = sim;
-                    tot = 0.0;
-                    esc = 0.0;
+                    etally[blockDim.x + tid] = 0.0;
+                    etally[tid] = 0.0;
                 }
                 const SimDesc& S = sd[sim];
                 rare_count(kRareLaunch);
@@ -1320,15 +1323,15 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         if (ev.term) {
             count_stopped(p);
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
-                tot += p.launchw;
-                esc += p.pw;
+                etally[blockDim.x + tid] += p.launchw;
+                etally[tid] += p.pw;
             }
             active = false;
         }
     }
-    if (tally_sim >= 0 && (tot != 0.0 || esc != 0.0)) {
-        atomicAdd(BP.tallies + 2 * tally_sim, esc);
-        atomicAdd(BP.tallies + 2 * tally_sim + 1, tot);
+    if (tally_sim >= 0 && (etally[blockDim.x + tid] != 0.0 || etally[tid] != 0.0)) {
+        atomicAdd(BP.tallies + 2 * tally_sim, etally[tid]);
+        atomicAdd(BP.tallies + 2 * tally_sim + 1, etally[blockDim.x + tid]);
     }
     flush_tallies(B, lane, 0.0, 0.0, c);
     rare_flush(B);
