@@ -48,6 +48,11 @@ CONFIG = {
 WORKLOAD = "heterogeneous forward, 60^3 grid, sphere R15, reflection on, 50 gates, 4 detectors (ppath saved)"
 METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates, 4 detectors)"
 
+# DRAM bytes (read + write) of one propagation launch of the default workload (1e7 photons), from an ncu capture
+# of the same command (dram__bytes_read.sum + dram__bytes_write.sum: 80.5 MB of label and table reads, 2.04 GB of
+# FP64-accumulator lines written back as L2 evicts them); not measured live, reported only for the default size
+DRAM_BYTES_DEFAULT_LAUNCH = 80_519_424 + 2_037_140_000
+
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
 # step L316-337, scatter L364-380, voxel crossing / deposit L285-310, reflect L381-417
 OPS_FP32 = {"steps": 26, "scatters": 45, "crossings": 8, "reflections": 25}
@@ -405,7 +410,8 @@ def run_gpu_arm(args) -> None:
             "kernel_ms": kms,
             "roofline": {"bound": "fp32", "achieved": achieved_fp32, "peak": peak_fp32,
                          "unit": "Top/s (FP32 instructions, FMA = 1 op; peak measured live by an FMA loop)",
-                         "frac": achieved_fp32 / peak_fp32, "traffic": None,
+                         "frac": achieved_fp32 / peak_fp32,
+                         "traffic": DRAM_BYTES_DEFAULT_LAUNCH if int(args.photons) == 10000000 else None,
                          "ops_per_launch": fp32_ops,
                          "events_per_launch": {k: int(getattr(r0, k)) for k in OPS_FP32},
                          "sfu": {"achieved": achieved_sfu, "peak": peak_sfu, "frac": achieved_sfu / peak_sfu,
