@@ -301,14 +301,14 @@ def run_gpu_arm(args) -> None:
     nout = nvox * sim.dim[3]
     d_lab = torch.from_numpy(job.labels.ravel().copy()).to(f"cuda:{device}")
     d_flu = torch.empty(nout, dtype=torch.float32, device=f"cuda:{device}")
-    d_det = torch.empty(sim.maxdetphotons * 4, dtype=torch.float32, device=f"cuda:{device}")
+    d_det = torch.empty(sim.maxdetphotons * detp_columns(sim), dtype=torch.float32, device=f"cuda:{device}")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
     stream = torch.cuda.current_stream()
     tuning = {"block_size": args.block, "blocks_per_sm": args.blocks_per_sm, "aggregation": args.aggregation,
               "source": "command line"}
     if not (args.block or args.blocks_per_sm or args.aggregation) and not args.no_autotune:
         # the project's autotuner: timed runs at half the photons over block sizes and aggregation modes.  A probe
-        # must be long against the launch's drain (the last, longest photons: ~8 ms here), or the drain's noise
+        # must be long against the launch's drain (the last, longest photons: ~7 ms here), or the drain's noise
         # decides the choice
         tuning = dict(ctx.autotune(sim, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.5),
                       source="autotune (50 % photon probes)")
