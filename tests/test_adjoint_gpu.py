@@ -194,3 +194,19 @@ def test_autograd_harness(ctx):
     fd = (L(mp) - L(mm)) / (2 * h)
     assert abs(mua.grad[k].item() - fd) <= 2e-3 * abs(fd)
     assert mus.grad is not None and torch.isfinite(mus.grad).all()
+
+
+def test_adjoint_budget_stops_kernel_and_context_survives(ctx):
+    """The adjoint forward kernel honours the launch budget too (status 3), and the context stays usable."""
+    from umcx_gb300 import Job
+
+    job = Job.from_args(["--bench", "cube60", "-n", "100000000"])
+    ctx.set_tuning(budget_ms=10)
+    try:
+        with pytest.raises(RuntimeError, match="status 3"):
+            ctx.forward_adjoint(job.sim, job.labels, job.media, job.detpos)
+    finally:
+        ctx.set_tuning()
+    small = Job.from_args(["--bench", "cube60", "-n", "10000"])
+    out = ctx.forward(small.sim, small.labels, small.media, small.detpos)
+    assert out.result.status == 0 and out.result.launched == 10000

@@ -116,3 +116,19 @@ def test_batch_outputs_into_caller_buffer(ctx):
     with pytest.raises(ValueError):
         b.get(0, out=np.zeros(10, np.float32))
     b.close()
+
+
+def test_batch_budget_stops_kernel_and_context_survives(ctx):
+    """A batch whose launch outlives its wall-clock budget stops with status 3 (no hang, no fault); the batch can be
+    re-tuned with a normal budget and run to completion, and the context stays usable."""
+    from umcx_gb300.api import Batch
+
+    jobs = small_batch(8, scale=0.5)
+    b = Batch.from_jobs(ctx, jobs)
+    b.set_tuning(1024, 0, 1, 1)  # 1 ms
+    with pytest.raises(RuntimeError, match="status 3.*budget"):
+        b.run()
+    b.set_tuning(1024, 0, 1, 0)
+    r = b.run()
+    assert r.status == 0 and r.launched == sum(j.sim.nphoton for j in jobs)
+    b.close()
