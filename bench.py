@@ -406,7 +406,8 @@ def run_gpu_arm(args) -> None:
                        "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},
-            "gpu_launches": args.steps,
+            # per step: the propagation kernel and the FP64 -> FP32 rounding of the output volume
+            "gpu_launches": args.steps * (2 if (sim.issavevol and not (sim.flags & 2)) else 1),
             "kernel_ms": kms,
             "roofline": {"bound": "fp32", "achieved": achieved_fp32, "peak": peak_fp32,
                          "unit": "Top/s (FP32 instructions, FMA = 1 op; peak measured live by an FMA loop)",
