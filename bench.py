@@ -279,6 +279,7 @@ def run_gpu_arm(args) -> None:
     import torch
 
     from umcx_gb300 import Context, Job, detp_columns, measure_peaks
+    from umcx_gb300._lib import SIM_FP32_ACCUM
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -407,7 +408,7 @@ def run_gpu_arm(args) -> None:
             "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},
             # per step: the propagation kernel and the FP64 -> FP32 rounding of the output volume
-            "gpu_launches": args.steps * (2 if (sim.issavevol and not (sim.flags & 2)) else 1),
+            "gpu_launches": args.steps * (2 if (sim.issavevol and not (sim.flags & SIM_FP32_ACCUM)) else 1),
             "kernel_ms": kms,
             "roofline": {"bound": "fp32", "achieved": achieved_fp32, "peak": peak_fp32,
                          "unit": "Top/s (FP32 instructions, FMA = 1 op; peak measured live by an FMA loop)",
