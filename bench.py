@@ -11,7 +11,8 @@ pathlengths saved.  Synthetic input (the configuration is generated, not read fr
 One step = one full simulation of P photons.  `value` is photons/ms of the propagation kernel with the inputs
 resident in HBM (CUDA events on the launching stream; the fluence output, 43 MB, is cleared inside the step and the
 L2 is flushed by writing a 256 MB buffer between steps).  `e2e` is the same metric through the C ABI call with host
-buffers (umcx_gpu_forward: label upload, simulation, fluence + detected-photon download), timed on the host.
+buffers in page-locked memory (umcx_gpu_forward: label upload, simulation, fluence + detected-photon download),
+timed on the host.
 
 --impl reference times the reference's own CPU implementation (the unmodified reference program built from its
 sources, oracle/_ref/umcx, with all host threads; else the C restatement in oracle/) on a bounded photon sample of
@@ -344,10 +345,16 @@ def run_gpu_arm(args) -> None:
     clocks = sampler.stop()
 
     # end to end through the C ABI with host buffers: the caller's label volume in, the fluence and detected-photon
-    # rows out into output arrays it reuses from call to call (allocated and touched once, outside the timed region)
-    h_lab, h_med, h_det = job.labels, job.media, job.detpos
-    h_flu = np.ones(nout, np.float32)
-    h_dp = np.ones(max(1, sim.maxdetphotons * detp_columns(sim)), np.float32)
+    # rows out into output arrays it reuses from call to call (page-locked host memory, allocated and touched once
+    # outside the timed region)
+    def pinned(n, dtype):
+        return torch.ones(n, dtype=dtype, pin_memory=True).numpy()
+
+    h_lab = pinned(nvox, torch.uint8)
+    h_lab[:] = job.labels.reshape(-1)
+    h_med, h_det = job.media, job.detpos
+    h_flu = pinned(nout, torch.float32)
+    h_dp = pinned(max(1, sim.maxdetphotons * detp_columns(sim)), torch.float32)
     e2e_ms = []
     for _ in range(max(1, args.e2e_steps)):
         flush.fill_(1)
