@@ -126,6 +126,9 @@ typedef struct umcx_context umcx_context;
 
 /* library ABI version (UMCX_ABI_VERSION) */
 int umcx_abi_version(void);
+/* 1 when the library was built with device bounds checks (UMCX_DEVICE_CHECKS=1: every indexed device-buffer access
+ * is tested first; a failing access is skipped and the call returns UMCX_ERR_CUDA naming it), else 0. */
+int umcx_device_checks(void);
 
 /* Create a context bound to CUDA device `device` (0-based; the reference's DeviceID is 1-based, L739). */
 int umcx_create(umcx_context** ctx, int device);

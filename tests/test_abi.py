@@ -34,6 +34,16 @@ def test_symbol_exported(name):
     assert hasattr(lib, name), f"{name} is declared in include/ but not exported by libumcx_gb300.so"
 
 
+def test_production_build_has_no_device_checks():
+    """The default build compiles the device bounds checks out (UMCX_DEVICE_CHECKS builds report 1)."""
+    import os
+
+    from umcx_gb300 import load
+
+    expect = 1 if "UMCX_DEVICE_CHECKS=1" in os.environ.get("UMCX_NVCC_DEFS", "") else 0
+    assert load().umcx_device_checks() == expect
+
+
 def test_python_signatures_cover_header():
     from umcx_gb300._lib import SIGNATURES
 

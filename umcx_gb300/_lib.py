@@ -119,6 +119,7 @@ _U8P = C.POINTER(C.c_uint8)
 # (name, restype, argtypes) of every exported entry point declared in include/*.h
 SIGNATURES = [
     ("umcx_abi_version", C.c_int, []),
+    ("umcx_device_checks", C.c_int, []),
     ("umcx_create", C.c_int, [C.POINTER(_P), C.c_int]),
     ("umcx_destroy", None, [_P]),
     ("umcx_last_error", C.c_char_p, [_P]),

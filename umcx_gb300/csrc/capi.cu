@@ -86,6 +86,17 @@ struct BudgetError : std::exception {
         if (e_ != cudaSuccess) throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));           \
     } while (0)
 
+// KStats::error of a finished launch is 0, UMCX_ERR_TIMEOUT (deadline reached) or kCheckError + site when a device
+// bounds check of a checked build (UMCX_DEVICE_CHECKS) failed; the last is an error of this library, reported as such
+int launch_status(int error) { return error >= kCheckError ? UMCX_ERR_CUDA : (error ? UMCX_ERR_TIMEOUT : UMCX_OK); }
+void throw_if_check_failed(int error) {
+    static const char* const kSites[] = {"label read", "medium of a label", "output deposit", "partial-path slot",
+                                         "detected-photon row", "Jacobian add"};
+    if (error < kCheckError) return;
+    const int site = error - kCheckError;
+    throw CudaError(std::string("device bounds check failed: ") + (site < 6 ? kSites[site] : "unknown access"));
+}
+
 template <class F>
 int guarded(umcx_context* ctx, F&& f) {
     try {
@@ -264,6 +275,9 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     B.labels = d_labels;
     B.fluence = d_fluence;
     B.detp = d_detp;
+    B.n_labels = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
+    B.n_out = s->issavevol ? nout : 0;
+    B.n_detp = d_detp ? static_cast<unsigned long long>(s->maxdetphotons) * umcx_detp_columns(s) : 0;
     B.media = static_cast<const Medium*>(ctx->media.ptr);
     B.stats = static_cast<KStats*>(ctx->stats.ptr);
     B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
@@ -303,9 +317,10 @@ void collect(umcx_context* ctx, const umcx_sim* s, cudaStream_t stream, umcx_res
         res->reflections = st.reflections;
         res->capped = st.capped;
         res->kernel_ms = ms;
-        res->status = st.error ? UMCX_ERR_TIMEOUT : UMCX_OK;
+        res->status = launch_status(st.error);
         res->label_bits = ctx->last_pack;
     }
+    throw_if_check_failed(st.error);
     if (st.error) throw BudgetError("propagation kernel stopped at its wall-clock budget; results are partial");
 }
 
@@ -314,6 +329,7 @@ void collect(umcx_context* ctx, const umcx_sim* s, cudaStream_t stream, umcx_res
 extern "C" {
 
 int umcx_abi_version(void) { return UMCX_ABI_VERSION; }
+int umcx_device_checks(void) { return UMCX_DEVICE_CHECKS != 0 ? 1 : 0; }
 
 int umcx_create(umcx_context** out, int device) {
     if (!out) return UMCX_ERR_INPUT;
@@ -388,30 +404,6 @@ int umcx_set_tuning(umcx_context* ctx, const umcx_tuning* t) {
         ctx->tuning = *t;
         return UMCX_OK;
     });
-}
-
-int umcx_seeds_from_rngseed(int32_t rngseed, uint32_t seeds[4]) {
-    if (!seeds) return UMCX_ERR_INPUT;
-    // srand(seed) followed by four rand() calls of the C library (L724-727), through the reentrant interface so
-    // the caller's own rand() state is left alone; rngseed <= 0 means "seed from the clock" like the reference
-    unsigned seed = rngseed > 0 ? static_cast<unsigned>(rngseed) : static_cast<unsigned>(std::time(nullptr));
-    struct random_data rd;
-    char state[128];
-    std::memset(&rd, 0, sizeof(rd));
-    std::memset(state, 0, sizeof(state));
-    if (initstate_r(seed, state, sizeof(state), &rd) != 0) return UMCX_ERR_INPUT;
-    for (int i = 0; i < 4; i++) {
-        int32_t v = 0;
-        random_r(&rd, &v);
-        seeds[i] = static_cast<uint32_t>(v);
-    }
-    return UMCX_OK;
-}
-
-int umcx_detp_columns(const umcx_sim* s) {
-    if (!s) return 0;
-    return (s->savedetflag & UMCX_DET_ID) + ((s->savedetflag & UMCX_DET_PPATH) > 0) * s->mediumnum +
-           (((s->savedetflag & UMCX_DET_EXITPOS) > 0) + ((s->savedetflag & UMCX_DET_EXITDIR) > 0)) * 3;
 }
 
 int umcx_gpu_forward_device(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labels, const float* media,
@@ -516,6 +508,9 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         B.fluence = s->issavevol ? static_cast<float*>(ctx->fluence.ptr) : nullptr;
         B.fluence64 = fp64 ? static_cast<double*>(ctx->accum64.ptr) : nullptr;
         B.detp = (cap * cols) ? static_cast<float*>(ctx->detp.ptr) : nullptr;
+        B.n_labels = nvox;
+        B.n_out = s->issavevol ? nout : 0;
+        B.n_detp = static_cast<unsigned long long>(cap) * cols;
         B.media = static_cast<const Medium*>(ctx->media.ptr);
         B.stats = static_cast<KStats*>(ctx->stats.ptr);
         B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
@@ -615,6 +610,8 @@ int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out) {
             B.replay_list = static_cast<const DetRecord*>(ctx->detrec.ptr);
             B.replay_count = n;
             B.jacobian = static_cast<float*>(ctx->jac.ptr);
+            B.n_labels = nvox;
+            B.n_jacobian = static_cast<unsigned long long>(s->detnum) * nvox;
             const int block = 128;
             int grid = static_cast<int>(std::min<unsigned long long>((n + block - 1) / block, 8ULL * ctx->sm_count));
             if (grid < 1) grid = 1;
@@ -628,6 +625,7 @@ int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out) {
             UMCX_CK(cudaStreamSynchronize(st));
             UMCX_CK(cudaEventElapsedTime(&out->replay_ms, ctx->ev0, ctx->ev1));
             out->replay_mismatch = stats.capped;
+            throw_if_check_failed(stats.error);
             if (stats.error) throw BudgetError("replay kernel stopped at its wall-clock budget");
         }
         UMCX_CK(cudaStreamSynchronize(st));
@@ -792,7 +790,7 @@ struct umcx_batch {
     int nsim = 0;
     std::vector<umcx_sim> sims;
     std::vector<unsigned long long> out_off, label_off;
-    unsigned long long nout_total = 0;
+    unsigned long long nout_total = 0, lab_total = 0;
     bool reflect = false, fp64 = true;
     struct Chunk {
         int first = 0, count = 0, media_first = 0, total_media = 0;
@@ -854,6 +852,8 @@ void batch_enqueue(umcx_batch* b, cudaStream_t st) {
         B.labels = static_cast<const uint8_t*>(b->labels.ptr);
         B.fluence = static_cast<float*>(b->out32.ptr);
         B.fluence64 = b->fp64 ? static_cast<double*>(b->out64.ptr) : nullptr;
+        B.n_labels = b->lab_total;
+        B.n_out = b->nout_total;
         B.media = static_cast<const Medium*>(b->media.ptr) + ch.media_first;
         B.stats = static_cast<KStats*>(b->stats.ptr);
         B.counter = static_cast<unsigned long long*>(b->counters.ptr) + c;
@@ -1016,6 +1016,7 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
         for (size_t c = 0; c < b->chunks.size(); c++) b->chunks[c].photons = totals[c];
         // device buffers
         UMCX_CK(b->labels.ensure(lab_total));
+        b->lab_total = lab_total;
         b->label_off = label_off;
         if (!labels) UMCX_CK(cudaMemset(b->labels.ptr, 0, lab_total));  // filled in place by the caller
         for (int i = 0; labels && i < nsim; i++) {
@@ -1075,8 +1076,9 @@ int umcx_batch_run(umcx_batch* b, umcx_result* total) {
             total->reflections = stats.reflections;
             total->capped = stats.capped;
             total->kernel_ms = ms;
-            total->status = stats.error ? UMCX_ERR_TIMEOUT : UMCX_OK;
+            total->status = launch_status(stats.error);
         }
+        throw_if_check_failed(stats.error);
         if (stats.error) throw BudgetError("batched kernel stopped at its wall-clock budget; results are partial");
         return UMCX_OK;
     });

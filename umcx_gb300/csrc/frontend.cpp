@@ -9,7 +9,9 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
@@ -808,3 +810,29 @@ Job make_job(const UserIO& io) {
 }
 
 }  // namespace umcx
+
+// host-side parts of the C ABI (umcx_gpu.h): the detected-photon record width (L157) and the session seeds
+// (L724-727)
+extern "C" int umcx_detp_columns(const umcx_sim* s) {
+    if (!s) return 0;
+    return (s->savedetflag & UMCX_DET_ID) + ((s->savedetflag & UMCX_DET_PPATH) > 0) * s->mediumnum +
+           (((s->savedetflag & UMCX_DET_EXITPOS) > 0) + ((s->savedetflag & UMCX_DET_EXITDIR) > 0)) * 3;
+}
+
+extern "C" int umcx_seeds_from_rngseed(int32_t rngseed, uint32_t seeds[4]) {
+    if (!seeds) return UMCX_ERR_INPUT;
+    // srand(seed) followed by four rand() calls of the C library (L724-727), through the reentrant interface so
+    // the caller's own rand() state is left alone; rngseed <= 0 means "seed from the clock" like the reference
+    unsigned seed = rngseed > 0 ? static_cast<unsigned>(rngseed) : static_cast<unsigned>(std::time(nullptr));
+    struct random_data rd;
+    char state[128];
+    std::memset(&rd, 0, sizeof(rd));
+    std::memset(state, 0, sizeof(state));
+    if (initstate_r(seed, state, sizeof(state), &rd) != 0) return UMCX_ERR_INPUT;
+    for (int i = 0; i < 4; i++) {
+        int32_t v = 0;
+        random_r(&rd, &v);
+        seeds[i] = static_cast<uint32_t>(v);
+    }
+    return UMCX_OK;
+}

@@ -70,7 +70,7 @@ struct KStats {
     unsigned long long scatters;
     unsigned long long reflections;
     unsigned long long capped;
-    int error;  // 0 ok, 3 deadline reached
+    int error;  // 0 ok, 3 deadline reached, kCheckError + site: a failed device bounds check (checked builds)
     int pad;
 };
 
@@ -119,7 +119,36 @@ struct KBuffers {
     const DetRecord* replay_list;  // replay input
     unsigned long long replay_count;
     float* jacobian;     // replay output [detnum][nx][ny][nz]
+    // element counts of the buffers above, read only by the device bounds checks of a checked build
+    unsigned long long n_labels, n_out, n_detp, n_jacobian;
 };
+
+// ---------------------------------------------------------------- device bounds checks (checked build variant)
+// Built with UMCX_DEVICE_CHECKS=1 (e.g. UMCX_NVCC_DEFS="UMCX_DEVICE_CHECKS=1"), the kernels test every indexed
+// access of a device buffer -- label reads (and the medium each label names), output deposits, partial-path slots,
+// detected-photon rows and Jacobian adds -- against the buffer's extent first.  An access outside it is skipped and
+// recorded in KStats::error as kCheckError + site (the first miss wins); the host turns it into an error naming the
+// site.  Production builds compile none of it.
+#ifndef UMCX_DEVICE_CHECKS
+#define UMCX_DEVICE_CHECKS 0
+#endif
+enum CheckSite { kSiteLabel = 0, kSiteMedium = 1, kSiteOutput = 2, kSitePath = 3, kSiteDetRow = 4, kSiteJacobian = 5 };
+constexpr int kCheckError = 16;
+
+// true when i < n; in a checked build a miss is recorded in *err and the caller skips the access
+__device__ __forceinline__ bool index_ok(int* err, unsigned long long i, unsigned long long n, int site) {
+    if constexpr (UMCX_DEVICE_CHECKS != 0) {
+        if (i >= n) {
+            atomicCAS(err, 0, kCheckError + site);
+            return false;
+        }
+    }
+    (void)err;
+    (void)i;
+    (void)n;
+    (void)site;
+    return true;
+}
 
 // ---------------------------------------------------------------- random numbers (MCX_rand, L187-215)
 struct Rng {
@@ -532,6 +561,8 @@ __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, con
 // one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
 // afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
 __device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v) {
+    if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), B.n_out, kSiteOutput))
+        return;
     if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
     else atomicAdd(B.fluence + idx, v);
 }
@@ -582,8 +613,36 @@ struct Event {
 // label bytes) in registers.
 struct GlobalLabels {
     const uint8_t* __restrict__ p;
-    __device__ __forceinline__ unsigned operator()(int i) const { return __ldg(p + i); }
+#if UMCX_DEVICE_CHECKS
+    unsigned long long n;  // voxels of the volume
+    unsigned nmedia;       // media of its table
+    int* err;
+#endif
+    __device__ __forceinline__ unsigned operator()(int i) const {
+#if UMCX_DEVICE_CHECKS
+        if (!index_ok(err, static_cast<unsigned long long>(static_cast<long long>(i)), n, kSiteLabel)) return 0u;
+        const unsigned v = __ldg(p + i);
+        return index_ok(err, v & UMCX_LABEL_MASK, nmedia, kSiteMedium) ? v : 0u;
+#else
+        return __ldg(p + i);
+#endif
+    }
 };
+// label view of n voxels at byte offset off of the label buffer, naming nmedia media
+__device__ __forceinline__ GlobalLabels global_labels(const KBuffers& B, unsigned long long off, unsigned long long n,
+                                                      unsigned nmedia) {
+    GlobalLabels g;
+    g.p = B.labels + off;
+#if UMCX_DEVICE_CHECKS
+    g.n = off + n <= B.n_labels ? n : 0;  // a view that overruns the buffer fails its first read
+    g.nmedia = nmedia;
+    g.err = &B.stats->error;
+#else
+    (void)n;
+    (void)nmedia;
+#endif
+    return g;
+}
 
 template <int BITS>
 struct PackedLabels {
@@ -776,6 +835,8 @@ __device__ __forceinline__ void append_detected(const KParams& P, const KBuffers
 // the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction]
 __device__ __forceinline__ void write_detp(const KParams& P, const KBuffers& B, const Photon& p, const float* ppath,
                                            unsigned stride, int d, unsigned long long slot) {
+    if (!index_ok(&B.stats->error, (slot + 1) * static_cast<unsigned long long>(P.cols), B.n_detp + 1, kSiteDetRow))
+        return;
     float* rec = B.detp + slot * static_cast<unsigned long long>(P.cols);
     int k = 0;
     if (P.savedetflag & UMCX_DET_ID) rec[k++] = static_cast<float>(d + 1);
@@ -874,7 +935,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
     unsigned* lwords = reinterpret_cast<unsigned*>(lwbuf + blockDim.x);
     typename LabelViewOf<PACK>::type labels;
     if constexpr (PACK == 0) {
-        labels.p = B.labels;
+        labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
     } else {
         const uint4* src = reinterpret_cast<const uint4*>(B.packed);
         uint4* dst = reinterpret_cast<uint4*>(lwords);
@@ -918,7 +979,8 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
 
         Event ev;
         advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c, active);  // no event on an idle lane
-        if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0)
+        if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0 &&
+            index_ok(&B.stats->error, ev.left_mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
             ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
         const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
         const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
@@ -977,6 +1039,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     double* etally = reinterpret_cast<double*>(Rk + K * bd);                    // [2][bd]: total, escape
     unsigned long long* cur = reinterpret_cast<unsigned long long*>(etally + 2 * bd);  // [bd]
     load_media(P, B.media, sm);
+    const GlobalLabels labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
 
     const unsigned tid = threadIdx.x;
     const unsigned lane = lane_id();
@@ -1005,7 +1068,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             } else {
                 rare_count(kRareLaunch);
                 cur[tid] = P.photon_offset + k;
-                active = start_photon<false>(P, GlobalLabels{B.labels}, p, P.photon_offset + k);
+                active = start_photon<false>(P, labels, p, P.photon_offset + k);
                 if (active) {
                     S = 0.f;
                     for (int q = 0; q < P.ppathlen; q++) ppath[q * bd + tid] = 0.f;
@@ -1031,10 +1094,12 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
         Event ev;
         ev.term = false;
         if (active) {
-            advance<false, REFLECT, true>(P, GlobalLabels{B.labels}, sm, p, ev, c);
+            advance<false, REFLECT, true>(P, labels, sm, p, ev, c);
             if (ev.crossed) {
                 const unsigned m = ev.left_mid;
-                if ((P.savedetflag & UMCX_DET_PPATH) && m > 0) ppath[(m - 1) * bd + tid] += ev.seg;
+                if ((P.savedetflag & UMCX_DET_PPATH) && m > 0 &&
+                    index_ok(&B.stats->error, m - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
+                    ppath[(m - 1) * bd + tid] += ev.seg;
                 float F = 0.f, dF = 0.f;
                 if (P.issavevol && ev.gate >= 0) {
                     dep_idx = ev.left_vox + ev.gate * static_cast<int>(P.dimxyz);
@@ -1130,6 +1195,7 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
     extern __shared__ float4 smem4[];
     Medium* sm = reinterpret_cast<Medium*>(smem4);
     load_media(P, B.media, sm);
+    const GlobalLabels labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
     const unsigned lane = lane_id();
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x, B.replay_count,
@@ -1151,7 +1217,7 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
             } else {
                 rec = B.replay_list[k];
                 rare_count(kRareLaunch);
-                active = start_photon<false>(P, GlobalLabels{B.labels}, p, rec.photon);
+                active = start_photon<false>(P, labels, p, rec.photon);
                 if (!active) mismatch++;
             }
         }
@@ -1162,10 +1228,10 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
         }
         if (active) {
             Event ev;
-            advance<false, REFLECT, true>(P, GlobalLabels{B.labels}, sm, p, ev, c);
-            if (ev.crossed && ev.left_vox >= 0)
-                atomicAdd(B.jacobian + static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox,
-                          -rec.weight * ev.seg);
+            advance<false, REFLECT, true>(P, labels, sm, p, ev, c);
+            const unsigned long long jidx = static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox;
+            if (ev.crossed && ev.left_vox >= 0 && index_ok(&B.stats->error, jidx, B.n_jacobian, kSiteJacobian))
+                atomicAdd(B.jacobian + jidx, -rec.weight * ev.seg);
             if (ev.term) {
                 count_stopped(p);
                 const bool same = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend && det_hit(P.det[rec.det - 1], p) &&
@@ -1209,6 +1275,7 @@ struct BParams {
 };
 
 __device__ __forceinline__ void deposit_add64(const KBuffers& B, long long idx, float v) {
+    if (!index_ok(&B.stats->error, static_cast<unsigned long long>(idx), B.n_out, kSiteOutput)) return;
     if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
     else atomicAdd(B.fluence + idx, v);
 }
@@ -1279,7 +1346,8 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 }
                 const SimDesc& S = sd[sim];
                 rare_count(kRareLaunch);
-                active = start_photon<false>(S, GlobalLabels{B.labels + S.label_off}, p, S.photon_offset + (g - begin[sim]));
+                const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
+                active = start_photon<false>(S, lab, p, S.photon_offset + (g - begin[sim]));
             }
         }
         // warp-uniform exits, tested every 16 iterations (a finished lane idles for at most 15 more)
@@ -1294,7 +1362,8 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         ev.term = false;
         if (active) {
             const SimDesc& S = sd[sim];
-            advance<false, REFLECT, false>(S, GlobalLabels{B.labels + S.label_off}, sm + S.media_base, p, ev, c);
+            const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
+            advance<false, REFLECT, false>(S, lab, sm + S.media_base, p, ev, c);
             const bool dep = ev.crossed && S.issavevol && ev.gate >= 0;
             dep_idx = dep ? static_cast<long long>(S.out_off) + ev.left_vox +
                                 static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz)
