@@ -88,13 +88,17 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     zlib = _have_zlib()
     hdrs = _headers()
     defs = ["-DUMCX_HAVE_ZLIB"] if zlib else []
+    # the CUDA objects of another build variant (different UMCX_NVCC_DEFS) are rebuilt
+    stamp = OUT / "nvcc_defs.txt"
+    variant = " ".join(_extra_defs())
+    rebuild_cu = not stamp.exists() or stamp.read_text() != variant
     steps = []
     objs = []
     for unit, extra in CU_UNITS.items():
         src = CSRC / unit
         obj = OUT / (unit + ".o")
         objs.append(obj)
-        if _stale(obj, [src, *hdrs]):
+        if rebuild_cu or _stale(obj, [src, *hdrs]):
             steps.append(([nvcc, *NVCC_FLAGS, *ARCH, *extra, *_extra_defs(), "-c", str(src), "-o", str(obj)],
                           OUT / (unit + ".log")))
     for unit in CPP_UNITS:
@@ -109,6 +113,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         for f in [ex.submit(_run, c, l) for c, l in steps]:
             f.result()
+    if rebuild_cu:
+        stamp.write_text(variant)
     if _stale(LIB, objs):
         libs = ["-lz"] if zlib else []
         _run([nvcc, "-shared", *ARCH, "-o", str(LIB), *map(str, objs), *libs], OUT / "link.log")
