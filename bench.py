@@ -213,7 +213,6 @@ def measure_adjoint(ctx, args) -> dict:
 def measure_batched(ctx, args, device) -> dict:
     """Batched form (configuration 5): 256 independent simulations in one persistent, graph-captured launch,
     autotuned, versus the same simulations as sequential single launches on the same GPU."""
-    import numpy as np
     import torch
 
     from umcx_gb300.api import Batch, autotune_batch
@@ -243,8 +242,9 @@ def measure_batched(ctx, args, device) -> dict:
     ms = statistics.mean(r.kernel_ms for r in runs)
     steps_per_photon = runs[-1].steps / max(1, runs[-1].launched)
     # end to end: one more run plus every simulation's output volume read back to the host, into one caller-owned
-    # buffer of the largest volume that is reused (allocated and touched outside the timed region)
-    host_out = np.ones(max(j.sim.dim[0] * j.sim.dim[1] * j.sim.dim[2] * j.sim.dim[3] for j in jobs), np.float32)
+    # page-locked buffer of the largest volume that is reused (allocated and touched outside the timed region)
+    host_out = torch.ones(max(j.sim.dim[0] * j.sim.dim[1] * j.sim.dim[2] * j.sim.dim[3] for j in jobs),
+                          dtype=torch.float32, pin_memory=True).numpy()
     t0 = time.perf_counter()
     b.run()
     out_bytes = 0
