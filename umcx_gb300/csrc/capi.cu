@@ -275,9 +275,8 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     B.labels = d_labels;
     B.fluence = d_fluence;
     B.detp = d_detp;
-    B.n_labels = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
-    B.n_out = s->issavevol ? nout : 0;
-    B.n_detp = d_detp ? static_cast<unsigned long long>(s->maxdetphotons) * umcx_detp_columns(s) : 0;
+    set_extents(B, 1ULL * s->dim[0] * s->dim[1] * s->dim[2], s->issavevol ? nout : 0,
+                d_detp ? static_cast<unsigned long long>(s->maxdetphotons) * umcx_detp_columns(s) : 0, 0);
     B.media = static_cast<const Medium*>(ctx->media.ptr);
     B.stats = static_cast<KStats*>(ctx->stats.ptr);
     B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
@@ -508,9 +507,7 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         B.fluence = s->issavevol ? static_cast<float*>(ctx->fluence.ptr) : nullptr;
         B.fluence64 = fp64 ? static_cast<double*>(ctx->accum64.ptr) : nullptr;
         B.detp = (cap * cols) ? static_cast<float*>(ctx->detp.ptr) : nullptr;
-        B.n_labels = nvox;
-        B.n_out = s->issavevol ? nout : 0;
-        B.n_detp = static_cast<unsigned long long>(cap) * cols;
+        set_extents(B, nvox, s->issavevol ? nout : 0, static_cast<unsigned long long>(cap) * cols, 0);
         B.media = static_cast<const Medium*>(ctx->media.ptr);
         B.stats = static_cast<KStats*>(ctx->stats.ptr);
         B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
@@ -610,8 +607,7 @@ int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out) {
             B.replay_list = static_cast<const DetRecord*>(ctx->detrec.ptr);
             B.replay_count = n;
             B.jacobian = static_cast<float*>(ctx->jac.ptr);
-            B.n_labels = nvox;
-            B.n_jacobian = static_cast<unsigned long long>(s->detnum) * nvox;
+            set_extents(B, nvox, 0, 0, static_cast<unsigned long long>(s->detnum) * nvox);
             const int block = 128;
             int grid = static_cast<int>(std::min<unsigned long long>((n + block - 1) / block, 8ULL * ctx->sm_count));
             if (grid < 1) grid = 1;
@@ -852,8 +848,7 @@ void batch_enqueue(umcx_batch* b, cudaStream_t st) {
         B.labels = static_cast<const uint8_t*>(b->labels.ptr);
         B.fluence = static_cast<float*>(b->out32.ptr);
         B.fluence64 = b->fp64 ? static_cast<double*>(b->out64.ptr) : nullptr;
-        B.n_labels = b->lab_total;
-        B.n_out = b->nout_total;
+        set_extents(B, b->lab_total, b->nout_total, 0, 0);
         B.media = static_cast<const Medium*>(b->media.ptr) + ch.media_first;
         B.stats = static_cast<KStats*>(b->stats.ptr);
         B.counter = static_cast<unsigned long long*>(b->counters.ptr) + c;

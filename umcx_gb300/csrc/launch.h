@@ -31,6 +31,23 @@ struct LaunchChoice {
     int pack = 0;  // bits per voxel of the shared-memory label copy (0 = labels read from global memory)
 };
 
+// buffer extents (elements) for the device bounds checks of a checked build; nothing in production builds
+inline void set_extents(KBuffers& B, unsigned long long labels, unsigned long long out, unsigned long long detp,
+                        unsigned long long jacobian) {
+#if UMCX_DEVICE_CHECKS
+    B.n_labels = labels;
+    B.n_out = out;
+    B.n_detp = detp;
+    B.n_jacobian = jacobian;
+#else
+    (void)B;
+    (void)labels;
+    (void)out;
+    (void)detp;
+    (void)jacobian;
+#endif
+}
+
 // dynamic shared memory of the forward kernel for a block size (pack > 0 adds the packed label copy)
 size_t forward_smem(const KParams& P, int block, bool savedet, int pack);
 

@@ -143,9 +143,8 @@ extern "C" int umcx_gpu_forward_noalloc(int device, const umcx_sim* s, const uin
     B.labels = d_labels;
     B.fluence = d_fluence;  // FP32 accumulation straight into the caller's output (no FP64 volume)
     B.detp = d_detp;
-    B.n_labels = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
-    B.n_out = s->issavevol ? B.n_labels * s->dim[3] : 0;
-    B.n_detp = d_detp ? static_cast<unsigned long long>(s->maxdetphotons) * umcx_detp_columns(s) : 0;
+    set_extents(B, 1ULL * s->dim[0] * s->dim[1] * s->dim[2], s->issavevol ? nout : 0,
+                d_detp ? static_cast<unsigned long long>(s->maxdetphotons) * umcx_detp_columns(s) : 0, 0);
     B.media = reinterpret_cast<const Medium*>(scratch + kMediaOff);
     B.stats = reinterpret_cast<KStats*>(scratch + kStatsOff);
     B.counter = reinterpret_cast<unsigned long long*>(scratch + kCounterOff);

@@ -103,6 +103,18 @@ struct KParams {
     float4 det[UMCX_MAX_DET];
 };
 
+// ---------------------------------------------------------------- device bounds checks (checked build variant)
+// Built with UMCX_DEVICE_CHECKS=1 (e.g. UMCX_NVCC_DEFS="UMCX_DEVICE_CHECKS=1"), the kernels test every indexed
+// access of a device buffer -- label reads (and the medium each label names), output deposits, partial-path slots,
+// detected-photon rows and Jacobian adds -- against the buffer's extent first.  An access outside it is skipped and
+// recorded in KStats::error as kCheckError + site (the first miss wins); the host turns it into an error naming the
+// site.  Production builds compile none of it.
+#ifndef UMCX_DEVICE_CHECKS
+#define UMCX_DEVICE_CHECKS 0
+#endif
+enum CheckSite { kSiteLabel = 0, kSiteMedium = 1, kSiteOutput = 2, kSitePath = 3, kSiteDetRow = 4, kSiteJacobian = 5 };
+constexpr int kCheckError = 16;
+
 struct KBuffers {
     const uint8_t* labels;
     const unsigned* packed;  // palette-packed labels (16-byte aligned, padded to whole uint4)
@@ -119,21 +131,19 @@ struct KBuffers {
     const DetRecord* replay_list;  // replay input
     unsigned long long replay_count;
     float* jacobian;     // replay output [detnum][nx][ny][nz]
-    // element counts of the buffers above, read only by the device bounds checks of a checked build
+#if UMCX_DEVICE_CHECKS
+    // element counts of the buffers above for the device bounds checks.  Checked builds only: extra kernel-parameter
+    // bytes alone changed the register allocation of the production adjoint kernel (spills)
     unsigned long long n_labels, n_out, n_detp, n_jacobian;
-};
-
-// ---------------------------------------------------------------- device bounds checks (checked build variant)
-// Built with UMCX_DEVICE_CHECKS=1 (e.g. UMCX_NVCC_DEFS="UMCX_DEVICE_CHECKS=1"), the kernels test every indexed
-// access of a device buffer -- label reads (and the medium each label names), output deposits, partial-path slots,
-// detected-photon rows and Jacobian adds -- against the buffer's extent first.  An access outside it is skipped and
-// recorded in KStats::error as kCheckError + site (the first miss wins); the host turns it into an error naming the
-// site.  Production builds compile none of it.
-#ifndef UMCX_DEVICE_CHECKS
-#define UMCX_DEVICE_CHECKS 0
 #endif
-enum CheckSite { kSiteLabel = 0, kSiteMedium = 1, kSiteOutput = 2, kSitePath = 3, kSiteDetRow = 4, kSiteJacobian = 5 };
-constexpr int kCheckError = 16;
+};
+// extent of a KBuffers buffer for index_ok (0 in production builds, where index_ok ignores it)
+#if UMCX_DEVICE_CHECKS
+#define UMCX_EXTENT(B, field) ((B).field)
+#else
+#define UMCX_EXTENT(B, field) 0ULL
+#endif
+
 
 // true when i < n; in a checked build a miss is recorded in *err and the caller skips the access
 __device__ __forceinline__ bool index_ok(int* err, unsigned long long i, unsigned long long n, int site) {
@@ -561,7 +571,8 @@ __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, con
 // one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
 // afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
 __device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v) {
-    if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), B.n_out, kSiteOutput))
+    if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), UMCX_EXTENT(B, n_out),
+                  kSiteOutput))
         return;
     if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
     else atomicAdd(B.fluence + idx, v);
@@ -835,7 +846,8 @@ __device__ __forceinline__ void append_detected(const KParams& P, const KBuffers
 // the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction]
 __device__ __forceinline__ void write_detp(const KParams& P, const KBuffers& B, const Photon& p, const float* ppath,
                                            unsigned stride, int d, unsigned long long slot) {
-    if (!index_ok(&B.stats->error, (slot + 1) * static_cast<unsigned long long>(P.cols), B.n_detp + 1, kSiteDetRow))
+    if (!index_ok(&B.stats->error, (slot + 1) * static_cast<unsigned long long>(P.cols), UMCX_EXTENT(B, n_detp) + 1,
+                  kSiteDetRow))
         return;
     float* rec = B.detp + slot * static_cast<unsigned long long>(P.cols);
     int k = 0;
@@ -1038,8 +1050,9 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     // touched once per photon, so kept out of the loop's registers: FP64 energy tallies and the photon index
     double* etally = reinterpret_cast<double*>(Rk + K * bd);                    // [2][bd]: total, escape
     unsigned long long* cur = reinterpret_cast<unsigned long long*>(etally + 2 * bd);  // [bd]
+    // the label view is built from kernel parameters where it is used, so it holds no registers in the loop
+    auto labels = [&]() { return global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)); };
     load_media(P, B.media, sm);
-    const GlobalLabels labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
 
     const unsigned tid = threadIdx.x;
     const unsigned lane = lane_id();
@@ -1068,7 +1081,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             } else {
                 rare_count(kRareLaunch);
                 cur[tid] = P.photon_offset + k;
-                active = start_photon<false>(P, labels, p, P.photon_offset + k);
+                active = start_photon<false>(P, labels(), p, P.photon_offset + k);
                 if (active) {
                     S = 0.f;
                     for (int q = 0; q < P.ppathlen; q++) ppath[q * bd + tid] = 0.f;
@@ -1094,7 +1107,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
         Event ev;
         ev.term = false;
         if (active) {
-            advance<false, REFLECT, true>(P, labels, sm, p, ev, c);
+            advance<false, REFLECT, true>(P, labels(), sm, p, ev, c);
             if (ev.crossed) {
                 const unsigned m = ev.left_mid;
                 if ((P.savedetflag & UMCX_DET_PPATH) && m > 0 &&
@@ -1195,7 +1208,6 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
     extern __shared__ float4 smem4[];
     Medium* sm = reinterpret_cast<Medium*>(smem4);
     load_media(P, B.media, sm);
-    const GlobalLabels labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
     const unsigned lane = lane_id();
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x, B.replay_count,
@@ -1217,7 +1229,8 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
             } else {
                 rec = B.replay_list[k];
                 rare_count(kRareLaunch);
-                active = start_photon<false>(P, labels, p, rec.photon);
+                active = start_photon<false>(P, global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)), p,
+                                             rec.photon);
                 if (!active) mismatch++;
             }
         }
@@ -1228,9 +1241,10 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
         }
         if (active) {
             Event ev;
-            advance<false, REFLECT, true>(P, labels, sm, p, ev, c);
+            advance<false, REFLECT, true>(P, global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)), sm,
+                                          p, ev, c);
             const unsigned long long jidx = static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox;
-            if (ev.crossed && ev.left_vox >= 0 && index_ok(&B.stats->error, jidx, B.n_jacobian, kSiteJacobian))
+            if (ev.crossed && ev.left_vox >= 0 && index_ok(&B.stats->error, jidx, UMCX_EXTENT(B, n_jacobian), kSiteJacobian))
                 atomicAdd(B.jacobian + jidx, -rec.weight * ev.seg);
             if (ev.term) {
                 count_stopped(p);
@@ -1275,7 +1289,7 @@ struct BParams {
 };
 
 __device__ __forceinline__ void deposit_add64(const KBuffers& B, long long idx, float v) {
-    if (!index_ok(&B.stats->error, static_cast<unsigned long long>(idx), B.n_out, kSiteOutput)) return;
+    if (!index_ok(&B.stats->error, static_cast<unsigned long long>(idx), UMCX_EXTENT(B, n_out), kSiteOutput)) return;
     if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
     else atomicAdd(B.fluence + idx, v);
 }
