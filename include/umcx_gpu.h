@@ -225,8 +225,8 @@ void umcx_batch_destroy(umcx_batch* b);
 
 /*
  * Autotuner (no reference counterpart): times short runs (sim's photons scaled by `fraction`, at least 20 000) of
- * the forward kernel over block sizes and fluence-aggregation modes, keeps the fastest in *best and installs it on
- * ctx.  Device buffers as for umcx_gpu_forward_device.
+ * the forward kernel over block sizes and fluence-aggregation modes (per candidate a warm-up run, then the fastest
+ * of three), keeps the fastest in *best and installs it on ctx.  Device buffers as for umcx_gpu_forward_device.
  */
 int umcx_autotune(umcx_context* ctx, const umcx_sim* sim, const uint8_t* d_labels, const float* media,
                   const float* detpos, float* d_fluence, float* d_detp, double fraction, umcx_tuning* best,
