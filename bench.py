@@ -54,6 +54,11 @@ METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates
 # FP64-accumulator lines written back as L2 evicts them); not measured live, reported only for the default size
 DRAM_BYTES_DEFAULT_LAUNCH = 80_519_424 + 2_037_140_000
 
+# warp instructions issued per voxel step by the propagation kernel, from an ncu capture of the default launch
+# (smsp__inst_executed.sum 4.20e10 over 3.436e9 steps; block 1024, plain atomics); with the live step count and
+# kernel time it gives the issue rate against the SMs' 4 issue slots per cycle (not measured live)
+WARP_INST_PER_STEP = 12.22
+
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
 # step L316-337, scatter L364-380, voxel crossing / deposit L285-310, reflect L381-417
 OPS_FP32 = {"steps": 26, "scatters": 45, "crossings": 8, "reflections": 25}
@@ -390,6 +395,8 @@ def run_gpu_arm(args) -> None:
     achieved_sfu = sfu_ops / (kms * 1e-3) / 1e12
     peak_sfu = peaks["sfu_per_s"] / 1e12
     atomics_per_s = r0.crossings / (kms * 1e-3)
+    issue_per_s = r0.steps * WARP_INST_PER_STEP / (kms * 1e-3)
+    issue_peak = peaks["sm_count"] * 4 * peaks["sm_clock_khz"] * 1e3
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     hbm_peak = json.loads(peaks_file.read_text()).get("hbm_gbs") if peaks_file.exists() else 6800.0
     traffic_alg = r0.crossings * 9.0  # label byte + fluence read-modify-write per crossing
@@ -427,7 +434,10 @@ def run_gpu_arm(args) -> None:
                                  "unit": "Top/s"},
                          "l2_atomics": {"achieved_per_s": atomics_per_s, "peak_per_s": peaks["l2_atomic_per_s"],
                                         "frac": atomics_per_s / peaks["l2_atomic_per_s"]},
-                         "hbm": {"algorithmic_gbs": traffic_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak}},
+                         "hbm": {"algorithmic_gbs": traffic_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak},
+                         "issue": {"achieved_warp_inst_per_s": issue_per_s, "peak_warp_inst_per_s": issue_peak,
+                                   "frac": issue_per_s / issue_peak, "warp_inst_per_step": WARP_INST_PER_STEP,
+                                   "source": "instructions per step from the ncu capture of the default launch"}},
             "clocks": clocks,
             "physics": {"absorbed_percent": (r0.energy_total - r0.energy_escape) / r0.energy_total * 100,
                         "detected": int(r0.detected), "steps_per_photon": r0.steps / r0.launched,
