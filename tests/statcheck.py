@@ -1,5 +1,5 @@
 """Statistical parity helpers: run the CUDA path and the CPU oracle on the same seeds, split into photon-index
-batches, and compare means with batch standard errors (spec tolerances: 3 standard errors)."""
+batches, and compare means with batch standard errors (parity tolerance: 3 standard errors)."""
 from __future__ import annotations
 
 import math

@@ -1,6 +1,6 @@
 """Parity of the CUDA forward path with the CPU oracle on the same inputs and seeds (GPU required).
 
-Spec tolerances: absorbed + escaped energy conserved to 1e-5 relative; detected-photon counts and
+Parity tolerances: absorbed + escaped energy conserved to 1e-5 relative; detected-photon counts and
 per-detector mean partial pathlengths within 3 standard errors; voxel fluence within 3 standard errors wherever a
 voxel has at least 100 deposits (the fraction of voxels beyond 3 SE must stay at the level chance allows), with the
 normalised L2 difference reported.  Standard errors come from photon-index batches of each run."""
