@@ -263,12 +263,7 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), stream));
     const size_t nout = 1ULL * s->dim[0] * s->dim[1] * s->dim[2] * s->dim[3];
     const bool fp64 = s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM);
-    if (fp64) {
-        UMCX_CK(ctx->accum64.ensure(nout * sizeof(double)));
-        UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, nout * sizeof(double), stream));
-    } else if (s->issavevol) {
-        UMCX_CK(cudaMemsetAsync(d_fluence, 0, nout * sizeof(float), stream));
-    }
+    if (s->issavevol && !fp64) UMCX_CK(cudaMemsetAsync(d_fluence, 0, nout * sizeof(float), stream));
 
     KBuffers B;
     std::memset(&B, 0, sizeof(B));
@@ -280,19 +275,29 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     B.media = static_cast<const Medium*>(ctx->media.ptr);
     B.stats = static_cast<KStats*>(ctx->stats.ptr);
     B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
-    B.fluence64 = fp64 ? static_cast<double*>(ctx->accum64.ptr) : nullptr;
     prepare_packed_labels(ctx, s, d_labels, P, B, stream);
 
     LaunchChoice lc = choose_launch(ctx->device, ctx->sm_count, ctx->tuning, s, P);
     P.aggregate = lc.aggregate;
+    // the FP64 accumulation volume, replicated when it is small (not with the packed-label kernels)
+    const unsigned reps = (fp64 && !lc.pack) ? accumulator_replicas(nout) : 1u;
+    if (fp64) {
+        UMCX_CK(ctx->accum64.ensure(reps * nout * sizeof(double)));
+        UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, reps * nout * sizeof(double), stream));
+        B.fluence64 = static_cast<double*>(ctx->accum64.ptr);
+        P.rep_mask = reps - 1;
+        P.rep_stride = static_cast<unsigned>(nout);
+        lc.repl = reps > 1;
+    }
     ctx->last_pack = lc.pack;
     if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
     UMCX_CK(cudaEventRecord(ctx->ev0, stream));
     launch_forward(lc, P, B, stream, (s->flags & UMCX_SIM_STRICT_MATH) != 0);
     UMCX_CK(cudaGetLastError());
     UMCX_CK(cudaEventRecord(ctx->ev1, stream));
-    if (fp64) {  // round the FP64 accumulation to the FP32 output once
-        launch_fp64_to_fp32(static_cast<const double*>(ctx->accum64.ptr), d_fluence, nout, ctx->sm_count, stream);
+    if (fp64) {  // round the FP64 accumulation (the sum of its replicas) to the FP32 output once
+        launch_fp64_to_fp32(static_cast<const double*>(ctx->accum64.ptr), d_fluence, nout, ctx->sm_count, stream,
+                            reps);
         UMCX_CK(cudaGetLastError());
     }
 }

@@ -100,6 +100,8 @@ struct KParams {
     unsigned palette[4];           // palette-packed labels: label byte of each code (4 bytes per word)
     unsigned packed_words;         // words of the packed label volume, a multiple of 4 (0 = not packed)
     int palette_bits;              // bits per voxel of the packed volume (2 or 4; 0 = not packed)
+    unsigned rep_mask;             // forward kernel: CTA b accumulates into FP64 replica (b & rep_mask) ...
+    unsigned rep_stride;           // ... which starts rep_stride elements after the previous one
     float4 det[UMCX_MAX_DET];
 };
 
@@ -569,16 +571,18 @@ __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, con
 }
 
 // one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
-// afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
-__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v) {
+// afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137).  rep_off selects
+// the CTA's replica of a replicated FP64 volume (0 otherwise).
+__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v, unsigned long long rep_off = 0) {
     if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), UMCX_EXTENT(B, n_out),
                   kSiteOutput))
         return;
-    if (B.fluence64) atomicAdd(B.fluence64 + idx, static_cast<double>(v));
+    if (B.fluence64) atomicAdd(B.fluence64 + rep_off + idx, static_cast<double>(v));
     else atomicAdd(B.fluence + idx, v);
 }
 
-__global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n);
+__global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n,
+                               unsigned reps);
 
 // =============================================================================================== loop building blocks
 struct Counters {
@@ -798,7 +802,8 @@ __device__ __forceinline__ bool det_hit(const float4 dp, const Photon& p) {  // 
 
 // fluence deposit of one iteration, called by all lanes of the warp (converged)
 __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggregate, float* aggbuf, unsigned tid,
-                                                  unsigned lane, int dep_idx, float dep_val) {
+                                                  unsigned lane, int dep_idx, float dep_val,
+                                                  unsigned long long rep_off = 0) {
     if (aggregate) {
         const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
         if (__popc(hm) > 1) {
@@ -809,13 +814,13 @@ __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggreg
                 float s = 0.f;
                 const unsigned base = tid & ~31u;
                 for (unsigned g = grp; g; g &= g - 1) s += aggbuf[base + __ffs(g) - 1];
-                deposit_add(B, dep_idx, s);
+                deposit_add(B, dep_idx, s, rep_off);
             }
             __syncwarp();
             return;
         }
     }
-    if (dep_idx >= 0) deposit_add(B, dep_idx, dep_val);
+    if (dep_idx >= 0) deposit_add(B, dep_idx, dep_val, rep_off);
 }
 
 // Detected-photon append (L276-278, L429-435; MCX_detect::addphoton L164-176), called only by the lanes of a warp
@@ -934,7 +939,8 @@ struct LabelViewOf<0> {
 #define UMCX_FWD_THREADS 1024
 #define UMCX_FWD_MINB 1
 #endif
-template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0>
+// REPL: the FP64 output volume is replicated (P.rep_mask, P.rep_stride; see accumulator_replicas)
+template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0, bool REPL = false>
 __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
@@ -997,7 +1003,8 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
         const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
         const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
         const float dep_val = dep ? ev.dep_val : 0.f;
-        deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val);
+        deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val,
+                          REPL ? static_cast<unsigned long long>(blockIdx.x & P.rep_mask) * P.rep_stride : 0ULL);
         if (ev.term) {
             count_stopped(p);
             if (SAVEDET) {
