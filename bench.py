@@ -201,7 +201,7 @@ def measure_adjoint(ctx, args) -> dict:
     job = Job.from_json(cfg)
     sim = job.sim
     fwd_ms, bwd_ms, recs = [], [], 0
-    for rep in range(3):
+    for rep in range(4):  # the first run warms up
         out = ctx.forward_adjoint(sim, job.labels, job.media, job.detpos)
         adj = ctx.backward(jacobian=True)
         if rep:
@@ -400,15 +400,17 @@ def run_gpu_arm(args) -> None:
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     hbm_peak = json.loads(peaks_file.read_text()).get("hbm_gbs") if peaks_file.exists() else 6800.0
     traffic_alg = r0.crossings * 9.0  # label byte + fluence read-modify-write per crossing
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_reference_run(args.cpu_photons, os.cpu_count() or 1)
+    # the other forms first, while the GPU is still at its working clock (the CPU baseline leaves it idle for
+    # seconds, and a cold start measured the adjoint form 15 % slow)
     forms = {}
     wanted = set() if args.no_forms else {f.strip() for f in args.forms.split(",") if f.strip()}
     if rank == 0 and "adjoint" in wanted:
         forms["adjoint"] = measure_adjoint(ctx, args)
     if rank == 0 and "batched" in wanted:
         forms["batched"] = measure_batched(ctx, args, device)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_reference_run(args.cpu_photons, os.cpu_count() or 1)
 
     if rank == 0:
         line = {

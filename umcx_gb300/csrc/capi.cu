@@ -280,14 +280,16 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     LaunchChoice lc = choose_launch(ctx->device, ctx->sm_count, ctx->tuning, s, P);
     P.aggregate = lc.aggregate;
     // the FP64 accumulation volume, replicated when it is small (not with the packed-label kernels)
-    const unsigned reps = (fp64 && !lc.pack) ? accumulator_replicas(nout) : 1u;
+    const Replicas reps = (fp64 && !lc.pack) ? accumulator_replicas(1ULL * s->dim[0] * s->dim[1] * s->dim[2], s->dim[3])
+                                             : Replicas{1u, 0ULL};
     if (fp64) {
-        UMCX_CK(ctx->accum64.ensure(reps * nout * sizeof(double)));
-        UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, reps * nout * sizeof(double), stream));
+        const size_t n64 = nout + (reps.copies - 1) * reps.len;
+        UMCX_CK(ctx->accum64.ensure(n64 * sizeof(double)));
+        UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, n64 * sizeof(double), stream));
         B.fluence64 = static_cast<double*>(ctx->accum64.ptr);
-        P.rep_mask = reps - 1;
-        P.rep_stride = static_cast<unsigned>(nout);
-        lc.repl = reps > 1;
+        P.rep_mask = reps.copies - 1;
+        P.rep_len = static_cast<unsigned>(reps.len);
+        lc.rep = reps.mode(nout);
     }
     ctx->last_pack = lc.pack;
     if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
@@ -500,7 +502,7 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), st));
         UMCX_CK(cudaMemsetAsync(ctx->grad.ptr, 0, 2 * K * sizeof(double), st));
         const bool fp64 = s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM);
-        if (fp64) {
+        if (fp64) {  // one copy: replicating the adjoint pass's volume measured no faster
             UMCX_CK(ctx->accum64.ensure(nout * sizeof(double)));
             UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, nout * sizeof(double), st));
         } else if (s->issavevol) {

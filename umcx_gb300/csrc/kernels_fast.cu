@@ -8,7 +8,8 @@ namespace umcx_dev {
 
 template <bool R, bool D>
 static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
-    if (lc.repl) k_forward<false, R, D, 0, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    if (lc.rep == kRepWhole) k_forward<false, R, D, 0, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.rep == kRepPrefix) k_forward<false, R, D, 0, kRepPrefix><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else k_forward<false, R, D><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
 }
 
@@ -34,8 +35,9 @@ static int occ_one(int block, size_t smem) {
 // benchmark configurations, 60 % was 2 % slower.
 template <bool R, bool D>
 static cudaError_t allow_big_smem() {
-    const cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D>);
-    return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, 0, true>) : e;
+    cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, 0, kRepPrefix>);
+    return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, 0, kRepWhole>) : e;
 }
 cudaError_t configure_fast_kernels() {
     cudaError_t e = allow_big_smem<false, false>();
@@ -109,30 +111,37 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     return lc;
 }
 
-// dst[i] = the FP64 sum of the reps replicas src[i], src[i + n], ... rounded once to FP32
+// dst[i] = the FP64 volume rounded once to FP32, its first len elements summed with their reps - 1 copies
+// (copy c of element i at n + (c - 1) * len + i)
 __global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n,
-                               unsigned reps) {
+                               unsigned reps, unsigned long long len) {
     const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
     for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += stride) {
         double v = src[i];
-        for (unsigned r = 1; r < reps; r++) v += src[i + r * n];
+        if (i < len)
+            for (unsigned r = 1; r < reps; r++) v += src[n + (r - 1) * len + i];
         dst[i] = static_cast<float>(v);
     }
 }
 
 void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream,
-                         unsigned reps) {
+                         Replicas reps) {
     if (n == 0) return;
     const unsigned long long blocks = (n + 255) / 256;
     const int grid = static_cast<int>(blocks < static_cast<unsigned long long>(sm_count) * 8 ? blocks : sm_count * 8ULL);
-    k_fp64_to_fp32<<<grid, 256, 0, stream>>>(src, dst, n, reps < 1 ? 1u : reps);
+    k_fp64_to_fp32<<<grid, 256, 0, stream>>>(src, dst, n, reps.copies, reps.copies > 1 ? reps.len : 0ULL);
 }
 
-unsigned accumulator_replicas(unsigned long long nout) {
+Replicas accumulator_replicas(unsigned long long nvox, unsigned maxgate) {
+    const unsigned long long nout = nvox * maxgate;
     unsigned k = 1;
     while (k < kMaxReplicas && 2ULL * k * nout * sizeof(double) <= kReplicaBytes) k *= 2;
-    return k;
+    if (k > 1) return Replicas{k, nout};
+    // a multi-gate volume: its first gates (the photons' first nanoseconds, still close to the source) in 4 copies
+    const unsigned long long gates = kReplicaBytes / sizeof(double) / (3ULL * nvox);
+    if (maxgate > 1 && gates >= 1) return Replicas{4u, (gates < maxgate ? gates : maxgate) * nvox};
+    return Replicas{1u, 0ULL};
 }
 
 __global__ void k_rng_dump(unsigned s0, unsigned s1, unsigned s2, unsigned s3, unsigned long long offset,

@@ -29,7 +29,7 @@ struct LaunchChoice {
     bool reflect = false;
     bool savedet = false;
     int pack = 0;  // bits per voxel of the shared-memory label copy (0 = labels read from global memory)
-    bool repl = false;  // replicated FP64 output volume (KParams::rep_mask > 0)
+    int rep = kRepNone;  // replication mode of the FP64 output volume (kRepPrefix / kRepWhole: KParams::rep_mask > 0)
 };
 
 // buffer extents (elements) for the device bounds checks of a checked build; nothing in production builds
@@ -109,17 +109,21 @@ void launch_mask_det(const int32_t* vol, const uint32_t dim[3], const DetLattice
 void launch_finish_labels(const int32_t* vol, const uint8_t* mark, unsigned long long n, int mediumnum,
                           uint8_t* out, unsigned long long* first_bad, int sm_count, cudaStream_t stream);
 
-void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream,
-                         unsigned reps = 1);
-
-// Replicated FP64 accumulation for small output volumes.  With a single time gate and a pencil beam every photon
-// deposits into the same few voxels below the source, and their atomics queue at a few L2 slices (see the forward
-// profile of that configuration).  The forward kernel then gives CTA b its own copy (b mod replicas) of the FP64
-// volume, which splits each hot voxel's atomics over that many addresses, and the rounding pass sums the copies.
-// Volumes up to kReplicaBytes in total (L2-resident) get up to kMaxReplicas copies; larger ones one.
+// Replicated FP64 accumulation.  With a pencil beam every photon deposits into the same few voxels below the
+// source, and their atomics queue at a few L2 slices (see the forward profile of the single-gate configuration).  The
+// forward kernel then gives CTA b its own copy (b mod copies) of the first `len` elements of the FP64 volume --
+// the whole volume when 8 copies fit in kReplicaBytes of L2, else (several gates) its first gates in 4 copies --
+// which splits each hot voxel's atomics over that many addresses; the rounding pass sums the copies.
 constexpr unsigned kMaxReplicas = 8;
 constexpr unsigned long long kReplicaBytes = 32ULL << 20;
-unsigned accumulator_replicas(unsigned long long nout);
+struct Replicas {
+    unsigned copies;         // 1: no copies
+    unsigned long long len;  // replicated elements at the start of the volume
+    int mode(unsigned long long nout) const { return copies < 2 ? kRepNone : (len >= nout ? kRepWhole : kRepPrefix); }
+};
+Replicas accumulator_replicas(unsigned long long nvox, unsigned maxgate);
+void launch_fp64_to_fp32(const double* src, float* dst, unsigned long long n, int sm_count, cudaStream_t stream,
+                         Replicas reps = Replicas{1u, 0ULL});
 
 void launch_rng_dump(const uint32_t seeds[4], unsigned long long offset, unsigned nphoton, unsigned ndraw, float* out,
                      cudaStream_t stream);

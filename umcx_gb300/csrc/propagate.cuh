@@ -100,8 +100,8 @@ struct KParams {
     unsigned palette[4];           // palette-packed labels: label byte of each code (4 bytes per word)
     unsigned packed_words;         // words of the packed label volume, a multiple of 4 (0 = not packed)
     int palette_bits;              // bits per voxel of the packed volume (2 or 4; 0 = not packed)
-    unsigned rep_mask;             // forward kernel: CTA b accumulates into FP64 replica (b & rep_mask) ...
-    unsigned rep_stride;           // ... which starts rep_stride elements after the previous one
+    unsigned rep_mask;             // forward kernel: CTA b deposits into copy c = b & rep_mask of the first rep_len
+    unsigned rep_len;              // elements of the FP64 volume (copy 0 is the volume itself; see accumulator_replicas)
     float4 det[UMCX_MAX_DET];
 };
 
@@ -570,19 +570,46 @@ __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, con
     }
 }
 
+// The CTA's copy of the replicated part of an FP64 volume: deposits below `len` go `base` elements further
+// (len = 0: no copy, every deposit goes to the volume itself).  Kernels are instantiated per replication mode:
+// kRepNone, kRepPrefix (the first gates are replicated: one compare per deposit) or kRepWhole (every element is).
+enum { kRepNone = 0, kRepPrefix = 1, kRepWhole = 2 };
+struct Replica {
+    unsigned len;
+    unsigned long long base;
+};
+template <int REP>
+__device__ __forceinline__ Replica cta_replica(const KParams& P) {
+    Replica r{0u, 0ULL};
+    if (REP != kRepNone) {  // copy c >= 1 of the CTA lies after the volume and copies 1 .. c-1; copy 0 is the volume
+        const unsigned c = blockIdx.x & P.rep_mask;
+        r.len = c ? P.rep_len : 0u;
+        r.base = c ? static_cast<unsigned long long>(P.dimxyz) * static_cast<unsigned>(P.maxgate) +
+                         static_cast<unsigned long long>(c - 1u) * P.rep_len
+                   : 0ULL;
+    }
+    return r;
+}
+
 // one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
-// afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137).  rep_off selects
-// the CTA's replica of a replicated FP64 volume (0 otherwise).
-__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v, unsigned long long rep_off = 0) {
+// afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
+template <int REP = kRepNone>
+__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v, Replica rep = Replica{0u, 0ULL}) {
     if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), UMCX_EXTENT(B, n_out),
                   kSiteOutput))
         return;
-    if (B.fluence64) atomicAdd(B.fluence64 + rep_off + idx, static_cast<double>(v));
-    else atomicAdd(B.fluence + idx, v);
+    if (B.fluence64) {
+        unsigned long long a = static_cast<unsigned long long>(idx);
+        if (REP == kRepWhole) a += rep.base;
+        if (REP == kRepPrefix) a += static_cast<unsigned>(idx) < rep.len ? rep.base : 0ULL;
+        atomicAdd(B.fluence64 + a, static_cast<double>(v));
+    } else {
+        atomicAdd(B.fluence + idx, v);
+    }
 }
 
 __global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict__ dst, unsigned long long n,
-                               unsigned reps);
+                               unsigned reps, unsigned long long len);
 
 // =============================================================================================== loop building blocks
 struct Counters {
@@ -801,9 +828,10 @@ __device__ __forceinline__ bool det_hit(const float4 dp, const Photon& p) {  // 
 }
 
 // fluence deposit of one iteration, called by all lanes of the warp (converged)
+template <int REP = kRepNone>
 __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggregate, float* aggbuf, unsigned tid,
                                                   unsigned lane, int dep_idx, float dep_val,
-                                                  unsigned long long rep_off = 0) {
+                                                  Replica rep = Replica{0u, 0ULL}) {
     if (aggregate) {
         const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
         if (__popc(hm) > 1) {
@@ -814,13 +842,13 @@ __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggreg
                 float s = 0.f;
                 const unsigned base = tid & ~31u;
                 for (unsigned g = grp; g; g &= g - 1) s += aggbuf[base + __ffs(g) - 1];
-                deposit_add(B, dep_idx, s, rep_off);
+                deposit_add<REP>(B, dep_idx, s, rep);
             }
             __syncwarp();
             return;
         }
     }
-    if (dep_idx >= 0) deposit_add(B, dep_idx, dep_val, rep_off);
+    if (dep_idx >= 0) deposit_add<REP>(B, dep_idx, dep_val, rep);
 }
 
 // Detected-photon append (L276-278, L429-435; MCX_detect::addphoton L164-176), called only by the lanes of a warp
@@ -939,8 +967,8 @@ struct LabelViewOf<0> {
 #define UMCX_FWD_THREADS 1024
 #define UMCX_FWD_MINB 1
 #endif
-// REPL: the FP64 output volume is replicated (P.rep_mask, P.rep_stride; see accumulator_replicas)
-template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0, bool REPL = false>
+// REP: replication mode of the FP64 output volume (P.rep_mask, P.rep_len; see accumulator_replicas)
+template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0, int REP = kRepNone>
 __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
@@ -975,6 +1003,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
     p.lastvox = -1;
     bool active = false, done = false;
     Counters c;
+    const Replica replica = cta_replica<REP>(P);
 
     for (unsigned iter = 0;; iter++) {
         if (!active && !done) {  // launch a photon on an idle lane (L761-763)
@@ -1003,8 +1032,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
         const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
         const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
         const float dep_val = dep ? ev.dep_val : 0.f;
-        deposit_converged(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val,
-                          REPL ? static_cast<unsigned long long>(blockIdx.x & P.rep_mask) * P.rep_stride : 0ULL);
+        deposit_converged<REP>(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val, replica);
         if (ev.term) {
             count_stopped(p);
             if (SAVEDET) {
