@@ -400,8 +400,7 @@ def run_gpu_arm(args) -> None:
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     hbm_peak = json.loads(peaks_file.read_text()).get("hbm_gbs") if peaks_file.exists() else 6800.0
     traffic_alg = r0.crossings * 9.0  # label byte + fluence read-modify-write per crossing
-    # the other forms first, while the GPU is still at its working clock (the CPU baseline leaves it idle for
-    # seconds, and a cold start measured the adjoint form 15 % slow)
+    # the other forms first, while the GPU is still busy (the CPU baseline leaves it idle for seconds)
     forms = {}
     wanted = set() if args.no_forms else {f.strip() for f in args.forms.split(",") if f.strip()}
     if rank == 0 and "adjoint" in wanted:
