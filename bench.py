@@ -50,14 +50,15 @@ WORKLOAD = "heterogeneous forward, 60^3 grid, sphere R15, reflection on, 50 gate
 METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates, 4 detectors)"
 
 # DRAM bytes (read + write) of one propagation launch of the default workload (1e7 photons), from an ncu capture
-# of the same command (dram__bytes_read.sum + dram__bytes_write.sum: 80.5 MB of label and table reads, 2.04 GB of
-# FP64-accumulator lines written back as L2 evicts them); not measured live, reported only for the default size
-DRAM_BYTES_DEFAULT_LAUNCH = 80_519_424 + 2_037_140_000
+# of the same command (dram__bytes_read.sum + dram__bytes_write.sum: 93.5 MB of label and table reads, 3.06 GB of
+# FP64-accumulator lines, the volume and the copies of its first gates, written back as L2 evicts them); not
+# measured live, reported only for the default size
+DRAM_BYTES_DEFAULT_LAUNCH = 93_477_376 + 3_064_464_000
 
 # warp instructions issued per voxel step by the propagation kernel, from an ncu capture of the default launch
-# (smsp__inst_executed.sum 4.20e10 over 3.436e9 steps; block 1024, plain atomics); with the live step count and
+# (smsp__inst_executed.sum 4.37e10 over 3.436e9 steps; block 1024, plain atomics); with the live step count and
 # kernel time it gives the issue rate against the SMs' 4 issue slots per cycle (not measured live)
-WARP_INST_PER_STEP = 12.22
+WARP_INST_PER_STEP = 12.72
 
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
 # step L316-337, scatter L364-380, voxel crossing / deposit L285-310, reflect L381-417
