@@ -279,7 +279,7 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
 
     LaunchChoice lc = choose_launch(ctx->device, ctx->sm_count, ctx->tuning, s, P);
     P.aggregate = lc.aggregate;
-    // the FP64 accumulation volume, replicated when it is small (not with the packed-label kernels)
+    // the FP64 accumulation volume with the copies of its hot part (accumulator_replicas; none with packed labels)
     const Replicas reps = (fp64 && !lc.pack) ? accumulator_replicas(1ULL * s->dim[0] * s->dim[1] * s->dim[2], s->dim[3])
                                              : Replicas{1u, 0ULL};
     if (fp64) {
