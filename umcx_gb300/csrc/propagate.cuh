@@ -576,17 +576,15 @@ __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, con
 enum { kRepNone = 0, kRepPrefix = 1, kRepWhole = 2 };
 struct Replica {
     unsigned len;
-    unsigned long long base;
+    unsigned base;  // below 2^32: the volume is below 2^31 elements and its copies below 4 Mi elements
 };
 template <int REP>
 __device__ __forceinline__ Replica cta_replica(const KParams& P) {
-    Replica r{0u, 0ULL};
+    Replica r{0u, 0u};
     if (REP != kRepNone) {  // copy c >= 1 of the CTA lies after the volume and copies 1 .. c-1; copy 0 is the volume
         const unsigned c = blockIdx.x & P.rep_mask;
         r.len = c ? P.rep_len : 0u;
-        r.base = c ? static_cast<unsigned long long>(P.dimxyz) * static_cast<unsigned>(P.maxgate) +
-                         static_cast<unsigned long long>(c - 1u) * P.rep_len
-                   : 0ULL;
+        r.base = c ? P.dimxyz * static_cast<unsigned>(P.maxgate) + (c - 1u) * P.rep_len : 0u;
     }
     return r;
 }
@@ -594,15 +592,19 @@ __device__ __forceinline__ Replica cta_replica(const KParams& P) {
 // one fluence deposit: into the FP64 accumulation volume when the launch has one (converted to the FP32 output
 // afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
 template <int REP = kRepNone>
-__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v, Replica rep = Replica{0u, 0ULL}) {
+__device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v, Replica rep = Replica{0u, 0u}) {
     if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), UMCX_EXTENT(B, n_out),
                   kSiteOutput))
         return;
     if (B.fluence64) {
-        unsigned long long a = static_cast<unsigned long long>(idx);
-        if (REP == kRepWhole) a += rep.base;
-        if (REP == kRepPrefix) a += static_cast<unsigned>(idx) < rep.len ? rep.base : 0ULL;
-        atomicAdd(B.fluence64 + a, static_cast<double>(v));
+        if (REP == kRepNone) {
+            atomicAdd(B.fluence64 + idx, static_cast<double>(v));
+        } else {  // 32-bit element offsets (idx >= 0 here)
+            unsigned a = static_cast<unsigned>(idx);
+            if (REP == kRepWhole) a += rep.base;
+            if (REP == kRepPrefix) a += a < rep.len ? rep.base : 0u;
+            atomicAdd(B.fluence64 + a, static_cast<double>(v));
+        }
     } else {
         atomicAdd(B.fluence + idx, v);
     }
@@ -831,7 +833,7 @@ __device__ __forceinline__ bool det_hit(const float4 dp, const Photon& p) {  // 
 template <int REP = kRepNone>
 __device__ __forceinline__ void deposit_converged(const KBuffers& B, bool aggregate, float* aggbuf, unsigned tid,
                                                   unsigned lane, int dep_idx, float dep_val,
-                                                  Replica rep = Replica{0u, 0ULL}) {
+                                                  Replica rep = Replica{0u, 0u}) {
     if (aggregate) {
         const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
         if (__popc(hm) > 1) {
