@@ -56,8 +56,9 @@ METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates
 DRAM_BYTES_DEFAULT_LAUNCH = 93_477_376 + 3_064_464_000
 
 # warp instructions issued per voxel step by the propagation kernel, from an ncu capture of the default launch
-# (smsp__inst_executed.sum 4.37e10 over 3.436e9 steps; block 1024, plain atomics); with the live step count and
-# kernel time it gives the issue rate against the SMs' 4 issue slots per cycle (not measured live)
+# (smsp__inst_executed.sum 4.37e10 over 3.436e9 steps; block 1024, plain atomics), captured before the copies of
+# the output volume took 32-bit offsets (a few instructions fewer per deposit, so a slight overestimate); with the
+# live step count and kernel time it gives the issue rate against the SMs' 4 issue slots per cycle
 WARP_INST_PER_STEP = 12.72
 
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
