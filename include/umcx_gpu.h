@@ -152,7 +152,9 @@ int umcx_detp_columns(const umcx_sim* sim);
  *   detpos   float [detnum][4]    = {x, y, z, radius} in voxels (may be NULL when detnum == 0)
  *   fluence  float [maxgate][nx][ny][nz], overwritten (may be NULL when issavevol == 0)
  *   detp     float [maxdetphotons][umcx_detp_columns(sim)] (may be NULL when issavedet == 0)
- * Copies in, runs the persistent propagation kernel, copies out, synchronises.
+ * Copies in, runs the persistent propagation kernel, copies out, synchronises.  Device memory held by ctx and
+ * reused by later calls: the label and output volumes, the detected-photon buffer, and unless UMCX_SIM_FP32_ACCUM
+ * the FP64 accumulation volume (8 bytes per output element) plus up to 32 MB of copies of its hot part.
  */
 int umcx_gpu_forward(umcx_context* ctx, const umcx_sim* sim, const uint8_t* labels, const float* media,
                      const float* detpos, float* fluence, float* detp, umcx_result* res);
