@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define UMCX_ABI_VERSION 2
+#define UMCX_ABI_VERSION 3
 
 /* status codes */
 enum {
@@ -106,7 +106,9 @@ typedef struct umcx_result {
     float kernel_ms;          /* device time of the propagation kernel (CUDA events) */
     float total_ms;           /* wall time of the whole call */
     int32_t status;           /* same as the return value */
-    int32_t label_bits;       /* bits per voxel of the shared-memory label copy the kernel read (0: global memory) */
+    int32_t block_size;       /* threads per CTA of the propagation launch */
+    int32_t grid_size;        /* CTAs of the propagation launch */
+    int32_t reserved;
 } umcx_result;
 
 /* Launch tuning; zero fields mean "choose automatically" (autotuner cache or built-in default). */
@@ -116,9 +118,10 @@ typedef struct umcx_tuning {
     int32_t aggregation;      /* 0 auto, 1 plain atomics, 2 warp match-any aggregation of fluence adds */
     int32_t budget_ms;        /* wall-clock budget of one propagation launch; 0 = 300 000 ms.  When it runs out the
                                  kernel stops, the call returns UMCX_ERR_TIMEOUT and the context stays usable. */
-    int32_t label_pack;       /* 0 or 1: labels from global memory; 2: from a palette-packed copy in shared memory
-                                 whenever it fits (at most 16 distinct label bytes, 2 or 4 bits per voxel, 192 KB).
-                                 The results are the same either way. */
+    int32_t grid_size;        /* CTAs of the launch; 0 = SM count x resident CTAs (one persistent wave).  A larger
+                                 grid is allowed: its later CTAs start as earlier ones finish.  The reference's
+                                 Session.ThreadNum / Session.BlockSize (-t / -T, L739-741) set it through
+                                 umcx_job_tuning. */
     int32_t reserved;         /* 0 */
 } umcx_tuning;
 
@@ -288,8 +291,11 @@ int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photo
  * library, held by every GPU that loads it until the process exits; at most UMCX_NOALLOC_MAX_MEDIA media fit, and
  * larger tables are rejected with UMCX_ERR_INPUT.  The output volume is accumulated in FP32 directly in d_fluence
  * (as with UMCX_SIM_FP32_ACCUM).  The first call on a device looks up that array's address; make it before any
- * stream capture.  All calls share the array: calls whose GPU work overlaps race and must be serialised by the
- * caller.  res->kernel_ms is 0 (no events).
+ * stream capture.  That address belongs to the device's primary context, so after the application resets the
+ * device (cudaDeviceReset) this entry point must not be called again in the process.  Each call synchronises its
+ * stream before returning (it reads the tallies back).  All calls share the array: calls whose GPU work overlaps
+ * race and must be serialised by the caller.  Inputs are checked by the same rules as umcx_gpu_forward_device.
+ * res->kernel_ms is 0 (no events).
  */
 #define UMCX_NOALLOC_SCRATCH_BYTES 8192
 #define UMCX_NOALLOC_MAX_MEDIA 128

@@ -47,6 +47,10 @@ const uint8_t* umcx_job_labels(const umcx_job* job);
 const float* umcx_job_media(const umcx_job* job);
 const float* umcx_job_detpos(const umcx_job* job);
 int umcx_job_isnormalized(const umcx_job* job);
+/* Launch shape the input asks for (Session.BlockSize / ThreadNum, the -T / -t flags; L739-741): block_size and
+ * grid_size set when either key is given, all zeros otherwise.  Pass it to umcx_set_tuning; the CLI and
+ * MCX_run_cmd / MCX_run_json do. */
+int umcx_job_tuning(const umcx_job* job, umcx_tuning* out);
 /* output normaliser for a total launched energy (L820) */
 float umcx_job_normalizer(const umcx_job* job, double energytotal);
 

@@ -27,23 +27,41 @@ REF_BIN = REF_DIR / "umcx"
 _lib = None
 
 
-def build(reference_root: str | None = "/root/reference") -> None:
-    """Compile the C oracle and (when its sources are reachable) the reference program."""
+def reference_root() -> Path | None:
+    """Checkout of the reference project: $UMCX_REFERENCE_ROOT, else a `reference` directory beside this repository;
+    None when neither holds src/umcx.cpp (on a host that only has the staged copy under oracle/_ref/)."""
+    for cand in (os.environ.get("UMCX_REFERENCE_ROOT"), str(HERE.parent.parent / "reference")):
+        if cand and Path(cand, "src", "umcx.cpp").exists():
+            return Path(cand)
+    return None
+
+
+def _ref_root_arg(root: str | None) -> str:
+    if root is None:
+        found = reference_root()
+        return str(found) if found else ""
+    return root
+
+
+def build(reference_root: str | None = None) -> None:
+    """Compile the C oracle and (when its sources are reachable) the reference program.  reference_root None looks
+    the checkout up (see reference_root()); "" uses only the staged copy."""
     BUILD.mkdir(exist_ok=True)
     src = HERE / "umcx_oracle.c"
     hdr = HERE.parent / "include" / "umcx_gpu.h"
     if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime):
         subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", str(LIB_PATH),
                         str(src), "-lm"], check=True)
-    if (reference_root and Path(reference_root, "src", "umcx.cpp").exists()) or (REF_DIR / "src" / "umcx.cpp").exists():
-        subprocess.run(["sh", str(HERE / "build_ref.sh"), reference_root or ""], check=True,
-                       stdout=subprocess.DEVNULL)
+    root = _ref_root_arg(reference_root)
+    if (root and Path(root, "src", "umcx.cpp").exists()) or (REF_DIR / "src" / "umcx.cpp").exists():
+        subprocess.run(["sh", str(HERE / "build_ref.sh"), root], check=True, stdout=subprocess.DEVNULL)
 
 
-def start_build_ref(reference_root: str | None = "/root/reference"):
+def start_build_ref(reference_root: str | None = None):
     """Start building the reference program in the background; returns the Popen (or None)."""
-    if (reference_root and Path(reference_root, "src", "umcx.cpp").exists()) or (REF_DIR / "src" / "umcx.cpp").exists():
-        return subprocess.Popen(["sh", str(HERE / "build_ref.sh"), reference_root or ""], stdout=subprocess.DEVNULL)
+    root = _ref_root_arg(reference_root)
+    if (root and Path(root, "src", "umcx.cpp").exists()) or (REF_DIR / "src" / "umcx.cpp").exists():
+        return subprocess.Popen(["sh", str(HERE / "build_ref.sh"), root], stdout=subprocess.DEVNULL)
     return None
 
 

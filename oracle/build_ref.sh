@@ -7,10 +7,12 @@
 # three source files are staged (unchanged) into oracle/_ref/src/, which is git-ignored but travels with the
 # working copy, and the binary is rebuilt there from that staged copy.  Nothing under oracle/_ref/ is committed.
 #
-# usage: sh oracle/build_ref.sh [REFERENCE_ROOT]      (default REFERENCE_ROOT=/root/reference)
+# usage: sh oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT: the reference checkout; default $UMCX_REFERENCE_ROOT, else a `reference` directory beside this
+#   repository.  Without one, the staged copy in oracle/_ref/src/ is built.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-/root/reference}
+REF=${1:-${UMCX_REFERENCE_ROOT:-$(dirname "$(dirname "$HERE")")/reference}}
 OUT="$HERE/_ref"
 mkdir -p "$OUT/src/nlohmann" "$OUT/src/zmat"
 if [ -f "$REF/src/umcx.cpp" ]; then

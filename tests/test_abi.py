@@ -56,7 +56,7 @@ def test_struct_layouts():
     from umcx_gb300._lib import Domain, Result, ShapeOp, Sim, Tuning
 
     assert C.sizeof(Sim) == 168
-    assert C.sizeof(Result) == 96
+    assert C.sizeof(Result) == 104
     assert C.sizeof(Tuning) == 24
     assert C.sizeof(ShapeOp) == 48
     assert C.sizeof(Domain) == 56

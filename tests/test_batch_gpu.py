@@ -1,4 +1,5 @@
-"""Batched simulations (one persistent, graph-captured launch) against single runs of the same simulations (GPU).
+"""Batched simulations (one persistent, graph-captured launch) against single runs of the same simulations and
+against the CPU oracle (GPU).
 
 Every photon of simulation i is seeded exactly as in a single run of i, so photon histories are the same up to the
 last bits of single-precision arithmetic (the batched and single kernels are separate compilations, which may
@@ -131,4 +132,74 @@ def test_batch_budget_stops_kernel_and_context_survives(ctx):
     b.set_tuning(1024, 0, 1, 0)
     r = b.run()
     assert r.status == 0 and r.launched == sum(j.sim.nphoton for j in jobs)
+    b.close()
+
+
+def stratified_subset():
+    """Indices of the 256-simulation workload covering every (edge, source type) stratum, alternating 2 and 5
+    tissue labels, plus one simulation with 3 and one with 4 labels."""
+    from umcx_gb300.workloads import EDGES, config5
+
+    cfgs = [config5(i) for i in range(256)]
+    info = [(c["Domain"]["Dim"][0], c["Optode"]["Source"]["Type"], len(c["Domain"]["Media"]) - 1) for c in cfgs]
+    picked = []
+    for k, (edge, stype) in enumerate((e, t) for e in EDGES for t in ("pencil", "isotropic")):
+        want = 2 if k % 2 == 0 else 5
+        cands = [i for i, (e, t, n) in enumerate(info) if e == edge and t == stype]
+        exact = [i for i in cands if info[i][2] == want]
+        picked.append((exact or cands)[0])
+    for nlab in (3, 4):
+        picked.append(next(i for i, (e, t, n) in enumerate(info) if n == nlab and i not in picked and e <= 64))
+    return picked
+
+
+def test_batched_form_matches_oracle(ctx):
+    """The batched kernel against the CPU oracle on the same seeds, for a stratified subset of the 256-simulation
+    workload (every domain edge, pencil and isotropic sources, 2 to 5 labels) at 1e5 photons each.  Each
+    simulation enters the batch as 10 photon-index ranges, so that both sides have batch standard errors; the
+    criteria are those of the single-simulation parity test: absorbed fraction within 3 standard errors, and over
+    voxels with at least 100 deposits at most frac_over3_limit(10) (2.3 %) beyond 3 standard errors, mean z^2 below
+    1.5, |mean z| below 0.2."""
+    import oracle
+    from statcheck import compare_fluence, run_batches, z_of_means
+    from test_forward_gpu import frac_over3_limit
+
+    from umcx_gb300.api import Batch
+    from umcx_gb300.workloads import batch5
+
+    idx = stratified_subset()
+    all_jobs = batch5(max(idx) + 1)
+    jobs = [all_jobs[i] for i in idx]
+    nb, photons = 10, 100000
+    per = photons // nb
+    entries, sims = [], []
+    for j in jobs:
+        s = j.sim
+        s.nphoton = photons
+        for k in range(nb):
+            t = s.copy()
+            t.photon_offset = k * per
+            t.nphoton = per
+            entries.append(j)
+            sims.append(t)
+    b = Batch.from_jobs(ctx, entries, sims=sims)
+    tot = b.run()
+    assert tot.status == 0 and tot.launched == nb * per * len(jobs)
+    for q, (i, j) in enumerate(zip(idx, jobs)):
+        s = j.sim
+        s.nphoton = photons
+        it = iter(range(q * nb, (q + 1) * nb))
+        g = run_batches(lambda _s: (lambda fr: (fr[0], None, fr[1]))(b.get(next(it))), s, nb)
+        c = run_batches(lambda _s: oracle.forward(_s, j.labels, j.media, None, depcount=True), s, nb)
+        zt = z_of_means(g.total, c.total)
+        assert abs(zt) < 3 or abs(g.total.sum() - c.total.sum()) <= 1e-6 * c.total.sum(), (i, zt)
+        za = z_of_means(g.absorbed, c.absorbed)
+        fc = compare_fluence(g, c, c.depcount)
+        line = (f"sim {i} (edge {s.dim[0]}, {s.mediumnum - 1} labels, src {s.srctype}): absorbed gpu "
+                f"{g.absorbed.mean():.5f} cpu {c.absorbed.mean():.5f} z={za:.2f}; voxels {fc.tested}, |z|>3 "
+                f"{fc.frac_over3:.4f}, max |z| {fc.max_abs_z:.2f}, mean z^2 {fc.mean_z2:.3f}, rel L2 {fc.rel_l2:.2e}")
+        print(line)
+        assert abs(za) < 3, line
+        if fc.tested:
+            assert fc.frac_over3 <= frac_over3_limit(nb) and fc.mean_z2 < 1.5 and abs(fc.mean_z) < 0.2, line
     b.close()

@@ -1,9 +1,15 @@
 """Parity of the CUDA forward path with the CPU oracle on the same inputs and seeds (GPU required).
 
-Parity tolerances: absorbed + escaped energy conserved to 1e-5 relative; detected-photon counts and
-per-detector mean partial pathlengths within 3 standard errors; voxel fluence within 3 standard errors wherever a
-voxel has at least 100 deposits (the fraction of voxels beyond 3 SE must stay at the level chance allows), with the
-normalised L2 difference reported.  Standard errors come from photon-index batches of each run."""
+Parity tolerances, as asserted below:
+  * energy: absorbed (the summed energy volume) + escaped = launched, to 1e-5 relative;
+  * absorbed fraction, launched energy, detected-photon count: within 3 standard errors (photon-index batches);
+  * per-detector mean partial pathlength of every label: within 3 standard errors (pooled detected rows);
+  * voxel fluence, over voxels with at least 100 deposits: the fraction beyond 3 standard errors at most three times
+    what chance gives for independent samples with batch standard errors (Student's t, frac_over3_limit: 1.4 % at 20
+    batches; the oracle and the GPU share photon seeds, which makes the differences smaller still), mean z^2 below
+    1.5 and |mean z| below 0.2; the normalised L2 difference and the largest |z| are printed for every case.
+Standard errors come from photon-index batches of each run.  The benchmark configurations run at their own photon
+counts (configuration 1 at 1e6, configuration 2 at 1e7, configuration 3 at 1e7 against its 1e8)."""
 import json
 import math
 import subprocess
@@ -39,19 +45,35 @@ def gpu_runner(ctx, job):
     return fn
 
 
-def cpu_runner(job):
+def cpu_runner(job, depcount=False):
     import oracle
 
     def fn(s):
-        f, d, r, _ = oracle.forward(s, job.labels, job.media, job.detpos)
-        return f, d, r
+        return oracle.forward(s, job.labels, job.media, job.detpos, depcount=depcount)
     return fn
 
 
+def frac_over3_limit(nbatch: int) -> float:
+    """Largest accepted fraction of tested voxels beyond 3 standard errors: three times what chance gives for
+    independent samples, whose z follows Student's t with 2 (nbatch - 1) degrees of freedom when both standard
+    errors come from nbatch batches (0.47 % at 20 batches, 0.77 % at 10), and at least 1 %."""
+    from scipy.stats import t
+
+    return max(0.01, 3 * 2 * float(t.sf(3.0, 2 * (nbatch - 1))))
+
+
+def with_output(spec, otype):
+    cfg = json.loads(json.dumps(spec))
+    cfg["Session"]["OutputType"] = otype
+    return cfg
+
+
 CASES = {
-    "c1": (C1, 200000, 20),
-    "c2": (C2, 200000, 20),
-    "c3": (C3, 200000, 10),
+    "c1": (C1, 1000000, 20),
+    "c2": (C2, 10000000, 20),
+    "c3": (C3, 10000000, 10),
+    "c1_fluence": (with_output(C1, "f"), 1000000, 20),
+    "c2_fluence": (with_output(C2, "f"), 1000000, 20),
     "cube60b": (["--bench", "cube60b"], 200000, 20),
     "spherebox": (["--bench", "spherebox"], 100000, 20),
     "sphshells": (["--bench", "sphshells"], 50000, 10),
@@ -69,13 +91,11 @@ CASES = {
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_forward_parity(ctx, name):
-    import oracle
-
     spec, n, nb = CASES[name]
     job = job_for(spec, n)
     sim = job.sim
     g = run_batches(gpu_runner(ctx, job), sim, nb)
-    c = run_batches(cpu_runner(job), sim, nb)
+    c = run_batches(cpu_runner(job, depcount=bool(sim.issavevol)), sim, nb)
     # every launched photon is processed exactly once
     assert sum(r.launched for r in g.results) == sim.nphoton
     assert all(r.status == 0 and r.capped == 0 for r in g.results)
@@ -83,41 +103,72 @@ def test_forward_parity(ctx, name):
     zt = z_of_means(g.total, c.total)
     assert abs(zt) < 3 or abs(g.total.sum() - c.total.sum()) <= 1e-6 * c.total.sum(), (g.total.sum(), c.total.sum())
     za = z_of_means(g.absorbed, c.absorbed)
-    assert abs(za) < 3, (name, g.absorbed.mean(), c.absorbed.mean(), za)
+    line = f"{name} ({sim.nphoton} photons): absorbed gpu {g.absorbed.mean():.6f} cpu {c.absorbed.mean():.6f} z={za:.2f}"
+    assert abs(za) < 3, line
     if sim.issavevol:
-        _, _, _, dep = oracle.forward(sim, job.labels, job.media, job.detpos, depcount=True)
-        fc = compare_fluence(g, c, dep)
-        print(f"{name}: absorbed gpu {g.absorbed.mean():.6f} cpu {c.absorbed.mean():.6f} z={za:.2f}; fluence "
-              f"voxels tested {fc.tested}, |z|>3 {fc.frac_over3:.4f}, mean z {fc.mean_z:.3f}, mean z^2 "
-              f"{fc.mean_z2:.3f}, rel L2 {fc.rel_l2:.2e}")
+        fc = compare_fluence(g, c, c.depcount)
+        line += (f"; fluence voxels tested {fc.tested}, |z|>3 {fc.frac_over3:.4f}, max |z| {fc.max_abs_z:.2f}, "
+                 f"mean z {fc.mean_z:.3f}, mean z^2 {fc.mean_z2:.3f}, rel L2 {fc.rel_l2:.2e}")
         if fc.tested:
-            assert fc.frac_over3 <= 0.02 and fc.mean_z2 < 1.5 and abs(fc.mean_z) < 0.2, fc
+            assert fc.frac_over3 <= frac_over3_limit(nb) and fc.mean_z2 < 1.5 and abs(fc.mean_z) < 0.2, line
     if sim.issavedet and sim.detnum:
         ng = sum(r.detected for r in g.results)
         nc = sum(r.detected for r in c.results)
-        assert abs(ng - nc) <= 3 * math.sqrt(ng + nc) + 1, (ng, nc)
-        if sim.savedetflag & 4:
-            cols = slice(1, 1 + sim.mediumnum) if sim.savedetflag & 1 else slice(0, sim.mediumnum)
-            if sim.savedetflag & 1:
-                for (n1, m1, s1), (n2, m2, s2) in zip(det_stats(g.detp, sim.detnum, cols),
-                                                      det_stats(c.detp, sim.detnum, cols)):
-                    assert abs(n1 - n2) <= 3 * math.sqrt(n1 + n2) + 1
-                    if n1 > 30 and n2 > 30:
-                        z = (m1 - m2) / np.sqrt(s1 ** 2 + s2 ** 2 + 1e-30)
-                        assert np.all(np.abs(z[np.isfinite(z)]) < 3.5), (name, m1, m2, z)
+        zd = (ng - nc) / math.sqrt(ng + nc) if ng + nc else 0.0
+        line += f"; detected gpu {ng} cpu {nc} z={zd:.2f}"
+        assert abs(zd) < 3, line
+        if sim.savedetflag & 4 and sim.savedetflag & 1:
+            cols = slice(1, 1 + sim.mediumnum)
+            zmax = 0.0
+            for (n1, m1, s1), (n2, m2, s2) in zip(det_stats(g.detp, sim.detnum, cols),
+                                                  det_stats(c.detp, sim.detnum, cols)):
+                zn = (n1 - n2) / math.sqrt(n1 + n2) if n1 + n2 else 0.0
+                assert abs(zn) < 3, (name, n1, n2)
+                if n1 > 30 and n2 > 30:
+                    z = (m1 - m2) / np.sqrt(s1 ** 2 + s2 ** 2 + 1e-30)
+                    z = z[np.isfinite(z)]
+                    zmax = max(zmax, float(np.abs(z).max()) if z.size else 0.0)
+                    assert np.all(np.abs(z) < 3), (name, m1, m2, z)
+            line += f"; per-detector mean partial path max |z| {zmax:.2f}"
+    print(line)
 
 
-def test_energy_conservation(ctx):
-    """Absorbed (sum of the FP32 energy volume) + escaped = launched, to 1e-5 relative (config 2 geometry)."""
-    cfg = json.loads(json.dumps(C2))
-    cfg["Session"].update({"OutputType": "e", "Photons": 1000000})
-    job = job_for(cfg, 1000000)
+@pytest.mark.parametrize("name,spec,photons", [
+    ("c1", C1, 10000000),    # configuration 1 geometry at 10x its photon count
+    ("c2", C2, 1000000),
+    ("c3", C3, 100000000),   # configuration 3 at its own photon count: 8 M voxels, ~2.7e10 deposits
+])
+def test_energy_conservation(ctx, name, spec, photons):
+    """Absorbed (the summed FP32 energy volume) + escaped = launched, to 1e-5 relative."""
+    cfg = json.loads(json.dumps(spec))
+    cfg["Session"].update({"OutputType": "e", "Photons": photons})
+    job = job_for(cfg, photons)
     out = ctx.forward(job.sim, job.labels, job.media, job.detpos)
     r = out.result
     absorbed = float(out.fluence.astype(np.float64).sum())
     rel = abs(absorbed + r.energy_escape - r.energy_total) / r.energy_total
-    print(f"energy: launched {r.energy_total:.3f} absorbed {absorbed:.3f} escaped {r.energy_escape:.3f} rel {rel:.2e}")
+    print(f"energy {name}: launched {r.energy_total:.3f} absorbed {absorbed:.3f} escaped {r.energy_escape:.3f} "
+          f"rel {rel:.2e}")
+    assert r.status == 0 and r.launched == photons
     assert rel < 1e-5
+
+
+def test_launch_shape_flags_on_gpu(ctx):
+    """-T 256 -t 25600 (BlockSize / ThreadNum, src/umcx.cpp:739-741) launch 100 CTAs of 256 threads; every photon's
+    history depends only on its index, so the event counts equal those of the default launch exactly."""
+    job = job_for(["--bench", "cubesph60b", "-T", "256", "-t", "25600"], 200000)
+    assert job.tuning == {"block_size": 256, "grid_size": 100}
+    base = ctx.forward(job.sim, job.labels, job.media, job.detpos).result
+    ctx.set_tuning(**job.tuning)
+    try:
+        r = ctx.forward(job.sim, job.labels, job.media, job.detpos).result
+    finally:
+        ctx.set_tuning()
+    assert (r.block_size, r.grid_size) == (256, 100)
+    assert base.block_size == 1024 and base.grid_size > 100
+    assert (r.launched, r.steps, r.crossings, r.scatters, r.reflections, r.detected) == (
+        base.launched, base.steps, base.crossings, base.scatters, base.reflections, base.detected)
+    assert abs(r.energy_escape - base.energy_escape) <= 1e-9 * base.energy_total
 
 
 def test_fp32_accumulation_mode(ctx):

@@ -125,3 +125,27 @@ def test_config_roundtrip():
     cfg = Job.from_args(["--bench", "skinvessel"]).config
     assert cfg["Domain"]["LengthUnit"] == 0.005 and cfg["Optode"]["Source"]["Type"] == "disk"
     assert list(cfg["Shapes"][2]["Cylinder"].keys()) == ["C0", "C1", "R", "Tag"]  # key-sorted literal (L647)
+
+
+@pytest.mark.parametrize("args,expect", [
+    ([], {}),                                                        # neither key: the library's own launch
+    (["-T", "256", "-t", "25600"], {"block_size": 256, "grid_size": 100}),
+    (["-T", "256"], {"block_size": 256, "grid_size": 390}),          # ThreadNum defaults to 100000 (L739)
+    (["-t", "6400"], {"block_size": 64, "grid_size": 100}),          # BlockSize defaults to 64 (L741)
+    (["-T", "100", "-t", "1000"], {"block_size": 128, "grid_size": 10}),  # rounded up to whole warps
+    (["--json", '{"Session":{"BlockSize":512,"ThreadNum":1000000}}'], {"block_size": 512, "grid_size": 1953}),
+])
+def test_launch_shape_flags(args, expect):
+    """-T/--blocksize and -t/--thread (Session.BlockSize / ThreadNum) set the launch shape as the reference's GPU
+    build does (src/umcx.cpp:739-741): CTAs of BlockSize threads, ThreadNum / BlockSize of them."""
+    from umcx_gb300 import Job
+
+    job = Job.from_args(["--bench", "cube60", "-n", "1000", *args])
+    assert job.tuning == expect
+
+
+def test_launch_shape_rejects_bad_block():
+    from umcx_gb300 import Job
+
+    with pytest.raises(ValueError, match="BlockSize"):
+        Job.from_args(["--bench", "cube60", "-n", "1000", "-T", "2048"])

@@ -69,7 +69,9 @@ class Result(C.Structure):
         ("kernel_ms", C.c_float),
         ("total_ms", C.c_float),
         ("status", C.c_int32),
-        ("label_bits", C.c_int32),
+        ("block_size", C.c_int32),
+        ("grid_size", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -78,7 +80,7 @@ class Result(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("aggregation", C.c_int32),
-                ("budget_ms", C.c_int32), ("label_pack", C.c_int32), ("reserved", C.c_int32)]
+                ("budget_ms", C.c_int32), ("grid_size", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Peaks(C.Structure):
@@ -160,6 +162,7 @@ SIGNATURES = [
     ("umcx_job_media", _FP, [_P]),
     ("umcx_job_detpos", _FP, [_P]),
     ("umcx_job_isnormalized", C.c_int, [_P]),
+    ("umcx_job_tuning", C.c_int, [_P, C.POINTER(Tuning)]),
     ("umcx_job_normalizer", C.c_float, [_P, C.c_double]),
     ("umcx_job_domain_dims", C.c_int, [_P, C.POINTER(C.c_uint32)]),
     ("umcx_job_domain_int32", C.c_int, [_P, _P, C.c_size_t]),

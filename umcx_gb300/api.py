@@ -112,6 +112,14 @@ class Job:
     def isnormalized(self) -> bool:
         return bool(load().umcx_job_isnormalized(self._h))
 
+    @property
+    def tuning(self) -> dict:
+        """Launch shape the input asks for (Session.BlockSize / ThreadNum, the -T / -t flags), as keyword arguments
+        of Context.set_tuning; empty when the input names neither."""
+        t = _lib.Tuning()
+        check(load().umcx_job_tuning(self._h, C.byref(t)), None, "umcx_job_tuning")
+        return {"block_size": t.block_size, "grid_size": t.grid_size} if (t.block_size or t.grid_size) else {}
+
     def normalizer(self, energytotal: float) -> float:
         return float(load().umcx_job_normalizer(self._h, energytotal))
 
@@ -210,10 +218,10 @@ class Context:
         return load().umcx_last_error(self._h).decode()
 
     def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0,
-                   budget_ms: int = 0, label_pack: int = 0) -> None:
-        """Launch tuning for later calls (0 = automatic).  label_pack: 1 reads labels from global memory, 2 from a
-        palette-packed copy in shared memory whenever it fits; results are identical either way."""
-        t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms, label_pack)
+                   budget_ms: int = 0, grid_size: int = 0) -> None:
+        """Launch tuning for later calls (0 = automatic).  grid_size: CTAs of the launch (0 = one persistent wave of
+        resident CTAs), as the reference's ThreadNum / BlockSize give it (Job.tuning)."""
+        t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms, grid_size)
         check(load().umcx_set_tuning(self._h, C.byref(t)), self._h, "umcx_set_tuning")
 
     def forward(self, sim: Sim, labels, media, detpos=None, fluence=None, detp=None) -> Forward:
@@ -314,7 +322,7 @@ class Context:
                                   C.byref(best), C.byref(ms))
         check(rc, self._h, "umcx_autotune")
         return {"block_size": best.block_size, "blocks_per_sm": best.blocks_per_sm, "aggregation": best.aggregation,
-                "label_pack": best.label_pack, "probe_ms": ms.value}
+                "probe_ms": ms.value}
 
     def rng_dump(self, seeds, photon_offset: int, nphoton: int, ndraw: int) -> np.ndarray:
         """rand01() draws [nphoton, ndraw] of photons photon_offset.. computed on the device (known-answer hook)."""

@@ -35,7 +35,6 @@ CU_UNITS = {
     "capi.cu": [],
     "kernels_fast.cu": FAST,
     "kernels_strict.cu": ["--fmad=false"],
-    "kernels_pack.cu": FAST,
     "kernels_adjoint.cu": FAST,
     "kernels_batch.cu": FAST,
     "peaks.cu": [],

@@ -15,6 +15,7 @@
 
 #include "../../include/umcx_gpu.h"
 #include "launch.h"
+#include "params.h"
 #include "propagate.cuh"
 
 using namespace umcx_dev;
@@ -51,9 +52,8 @@ struct umcx_context {
     std::string err;
     umcx_tuning tuning{};
     DevBuf labels, fluence, detp, media, stats, counter, scratch, accum64;
-    DevBuf packed, presence;  // palette-packed label copy and the 256-bit label-byte set it is planned from
     DevBuf raster, raster_ops, raster_coords;  // device label builder: int32 volume + marks + flags, ops, lattices
-    int last_pack = 0;        // bits per voxel of the label copy the last forward launch read (0 = global labels)
+    int last_block = 0, last_grid = 0;  // launch shape of the last propagation launch (reported in umcx_result)
     // adjoint state kept between umcx_gpu_forward_adjoint and umcx_gpu_backward
     DevBuf detrec, detext, grad, jac;
     umcx_sim adj_sim{};
@@ -124,122 +124,10 @@ int guarded(umcx_context* ctx, F&& f) {
 }
 
 void validate(const umcx_sim* s) {
-    if (!s) throw InputError("sim is NULL");
-    if (s->flags & ~UMCX_SIM_FLAGS_ALL) throw InputError("unknown bits in umcx_sim.flags");
-    for (int k = 0; k < 3; k++)
-        if (s->dim[k] < 1 || s->dim[k] > 32767) throw InputError("dim[0..2] must be in 1..32767");
-    if (s->dim[3] < 1 || s->dim[3] > UMCX_MAX_GATES) throw InputError("dim[3] (time gates) must be in 1..65535");
-    const unsigned long long nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
-    if (nvox * s->dim[3] >= (1ULL << 31)) throw InputError("voxels x gates must be below 2^31");
-    if (s->mediumnum < 1 || s->mediumnum > UMCX_MAX_MEDIA) throw InputError("mediumnum must be in 1..128");
-    if (s->detnum < 0 || s->detnum > UMCX_MAX_DET) throw InputError("detnum must be in 0..64");
-    if (!(s->rtstep > 0.f) || !std::isfinite(s->tend)) throw InputError("invalid time window");
-    if (s->srctype < 0 || s->srctype > 6) throw InputError("unknown source type");
-}
-
-Medium make_medium(const float* m, int outputtype) {
-    Medium r;
-    const float mua = m[0], mus = m[1], g = m[2], n = m[3];
-    r.a = make_float4(mua, mus, g, n);
-    r.b = make_float4(mus != 0.f ? 1.f / mus : 0.f, deposit_factor(mua, outputtype), g != 0.f ? 1.f / (2.f * g) : 0.f,
-                      n * kOneOverC0);
-    r.c = make_float4(1.f - g * g, 1.f - g, 2.f * g, 1.f + g * g);
-    return r;
-}
-
-KParams make_params(const umcx_sim* s, const float* detpos) {
-    KParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.nx = static_cast<int>(s->dim[0]);
-    P.ny = static_cast<int>(s->dim[1]);
-    P.nz = static_cast<int>(s->dim[2]);
-    P.maxgate = static_cast<int>(s->dim[3]);
-    P.dimyz = s->dim[1] * s->dim[2];
-    P.dimxyz = P.dimyz * s->dim[0];
-    P.nphoton = s->nphoton;
-    P.photon_offset = s->photon_offset;
-    P.tstart = s->tstart;
-    P.tend = s->tend;
-    P.rtstep = s->rtstep;
-    P.unitinmm = s->unitinmm;
-    P.isreflect = s->isreflect;
-    P.issavevol = s->issavevol;
-    P.issavedet = s->issavedet;
-    P.savedetflag = s->savedetflag;
-    P.mediumnum = s->mediumnum;
-    P.outputtype = s->outputtype;
-    P.detnum = s->detnum;
-    P.srctype = s->srctype;
-    P.maxdetphotons = s->issavedet ? s->maxdetphotons : 0u;
-    P.cols = umcx_detp_columns(s);
-    P.ppathlen = (s->issavedet && (s->savedetflag & UMCX_DET_PPATH)) ? s->mediumnum : 0;
-    P.step_cap = kDefaultStepCap;
-    for (int k = 0; k < 4; k++) P.seeds[k] = s->seeds[k];
-    P.srcpos = make_float4(s->srcpos[0], s->srcpos[1], s->srcpos[2], 1.f);
-    P.srcdir = make_float4(s->srcdir[0], s->srcdir[1], s->srcdir[2], 0.f);
-    P.srcrdir = make_float4(1.f / s->srcdir[0], 1.f / s->srcdir[1], 1.f / s->srcdir[2], 0.f);
-    P.srcparam1 = make_float4(s->srcparam1[0], s->srcparam1[1], s->srcparam1[2], s->srcparam1[3]);
-    P.srcparam2 = make_float4(s->srcparam2[0], s->srcparam2[1], s->srcparam2[2], s->srcparam2[3]);
-    P.budget_ns = 300ULL * 1000000000ULL;  // 5 minutes (umcx_tuning.budget_ms overrides)
-    for (int d = 0; d < s->detnum; d++)
-        P.det[d] = make_float4(detpos[4 * d], detpos[4 * d + 1], detpos[4 * d + 2], detpos[4 * d + 3]);
-    return P;
+    if (const char* why = check_sim(s)) throw InputError(why);
 }
 
 void set_device(umcx_context* ctx) { UMCX_CK(cudaSetDevice(ctx->device)); }
-
-// Palette-packed label copies are planned up to this size (the forward kernel holds one per CTA in shared memory).
-constexpr unsigned long long kMaxPackedBytes = 192ULL * 1024ULL;
-
-// Palette of the label bytes present (mask: 256-bit set) and the code of each: at most 16 distinct bytes, 2 bits
-// per voxel for up to 4 of them, else 4.  Fills P.palette / palette_bits / packed_words; false if it cannot pack.
-bool plan_palette(const unsigned mask[8], unsigned long long nvox, LabelCodes& codes, KParams& P) {
-    int distinct = 0;
-    unsigned bytes[16];
-    for (unsigned b = 0; b < 256u; b++) {
-        if (!((mask[b >> 5] >> (b & 31u)) & 1u)) continue;
-        if (distinct == 16) return false;
-        bytes[distinct++] = b;
-    }
-    if (distinct == 0) return false;
-    const int bits = distinct <= 4 ? 2 : 4;
-    const unsigned long long per = 32ULL / static_cast<unsigned>(bits);
-    unsigned long long words = (nvox + per - 1) / per;
-    words = (words + 3ULL) & ~3ULL;  // the kernel stages whole 16-byte vectors
-    if (words * sizeof(unsigned) > kMaxPackedBytes) return false;
-    std::memset(codes.c, 0, sizeof(codes.c));
-    std::memset(P.palette, 0, sizeof(P.palette));
-    for (int k = 0; k < distinct; k++) {
-        codes.c[bytes[k]] = static_cast<uint8_t>(k);
-        P.palette[k >> 2] |= bytes[k] << ((k & 3) * 8);
-    }
-    P.palette_bits = bits;
-    P.packed_words = static_cast<unsigned>(words);
-    return true;
-}
-
-// Build the palette-packed label copy for the fast forward kernel when the volume is small enough and has few label
-// bytes: one scan of the labels for the set of bytes present (read back to choose the palette), one packing pass.
-void prepare_packed_labels(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labels, KParams& P, KBuffers& B,
-                           cudaStream_t stream) {
-    if (ctx->tuning.label_pack != 2 || (s->flags & UMCX_SIM_STRICT_MATH)) return;
-    const unsigned long long nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
-    if (nvox > kMaxPackedBytes * 4ULL) return;  // does not fit even at 2 bits per voxel
-    UMCX_CK(ctx->presence.ensure(8 * sizeof(unsigned)));
-    UMCX_CK(cudaMemsetAsync(ctx->presence.ptr, 0, 8 * sizeof(unsigned), stream));
-    launch_label_presence(d_labels, nvox, static_cast<unsigned*>(ctx->presence.ptr), ctx->sm_count, stream);
-    UMCX_CK(cudaGetLastError());
-    unsigned mask[8];
-    UMCX_CK(cudaMemcpyAsync(mask, ctx->presence.ptr, sizeof(mask), cudaMemcpyDeviceToHost, stream));
-    UMCX_CK(cudaStreamSynchronize(stream));
-    LabelCodes codes;
-    if (!plan_palette(mask, nvox, codes, P)) return;
-    UMCX_CK(ctx->packed.ensure(P.packed_words * sizeof(unsigned)));
-    launch_label_pack(d_labels, nvox, P.palette_bits, codes, static_cast<unsigned*>(ctx->packed.ptr), P.packed_words,
-                      ctx->sm_count, stream);
-    UMCX_CK(cudaGetLastError());
-    B.packed = static_cast<const unsigned*>(ctx->packed.ptr);
-}
 
 // Enqueue one forward simulation on `stream`: clears the tallies and the output, launches the propagation kernel
 // between the context's two events.  All buffers are device buffers.
@@ -275,13 +163,12 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
     B.media = static_cast<const Medium*>(ctx->media.ptr);
     B.stats = static_cast<KStats*>(ctx->stats.ptr);
     B.counter = static_cast<unsigned long long*>(ctx->counter.ptr);
-    prepare_packed_labels(ctx, s, d_labels, P, B, stream);
 
     LaunchChoice lc = choose_launch(ctx->device, ctx->sm_count, ctx->tuning, s, P);
     P.aggregate = lc.aggregate;
-    // the FP64 accumulation volume with the copies of its hot part (accumulator_replicas; none with packed labels)
-    const Replicas reps = (fp64 && !lc.pack) ? accumulator_replicas(1ULL * s->dim[0] * s->dim[1] * s->dim[2], s->dim[3])
-                                             : Replicas{1u, 0ULL};
+    // the FP64 accumulation volume with the copies of its hot part (accumulator_replicas)
+    const Replicas reps = fp64 ? accumulator_replicas(1ULL * s->dim[0] * s->dim[1] * s->dim[2], s->dim[3])
+                               : Replicas{1u, 0ULL};
     if (fp64) {
         const size_t n64 = nout + (reps.copies - 1) * reps.len;
         UMCX_CK(ctx->accum64.ensure(n64 * sizeof(double)));
@@ -291,7 +178,8 @@ void enqueue_forward(umcx_context* ctx, const umcx_sim* s, const uint8_t* d_labe
         P.rep_len = static_cast<unsigned>(reps.len);
         lc.rep = reps.mode(nout);
     }
-    ctx->last_pack = lc.pack;
+    ctx->last_block = lc.block;
+    ctx->last_grid = lc.grid;
     if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
     UMCX_CK(cudaEventRecord(ctx->ev0, stream));
     launch_forward(lc, P, B, stream, (s->flags & UMCX_SIM_STRICT_MATH) != 0);
@@ -324,7 +212,8 @@ void collect(umcx_context* ctx, const umcx_sim* s, cudaStream_t stream, umcx_res
         res->capped = st.capped;
         res->kernel_ms = ms;
         res->status = launch_status(st.error);
-        res->label_bits = ctx->last_pack;
+        res->block_size = ctx->last_block;
+        res->grid_size = ctx->last_grid;
     }
     throw_if_check_failed(st.error);
     if (st.error) throw BudgetError("propagation kernel stopped at its wall-clock budget; results are partial");
@@ -354,7 +243,6 @@ int umcx_create(umcx_context** out, int device) {
         UMCX_CK(cudaEventCreate(&ctx->ev1));
         UMCX_CK(configure_fast_kernels());
         UMCX_CK(configure_strict_kernels());
-        UMCX_CK(configure_packed_kernels());
         UMCX_CK(configure_adjoint_kernels());
         return UMCX_OK;
     });
@@ -378,8 +266,6 @@ void umcx_destroy(umcx_context* ctx) {
     ctx->counter.release();
     ctx->scratch.release();
     ctx->accum64.release();
-    ctx->packed.release();
-    ctx->presence.release();
     ctx->raster.release();
     ctx->raster_ops.release();
     ctx->raster_coords.release();
@@ -407,6 +293,7 @@ int umcx_set_tuning(umcx_context* ctx, const umcx_tuning* t) {
         if (t->blocks_per_sm < 0 || t->blocks_per_sm > 32) throw InputError("blocks_per_sm must be in 0..32");
         if (t->aggregation < 0 || t->aggregation > 2) throw InputError("aggregation must be 0, 1 or 2");
         if (t->budget_ms < 0) throw InputError("budget_ms must be >= 0");
+        if (t->grid_size < 0 || t->grid_size > (1 << 24)) throw InputError("grid_size must be in 0..2^24");
         ctx->tuning = *t;
         return UMCX_OK;
     });
@@ -530,13 +417,14 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         if (smem > kMaxDynamicSmem) throw InputError("too many media for the adjoint's per-thread tallies");
         int occ = adjoint_occupancy(s->isreflect != 0, block, smem);
         if (occ < 1) occ = 1;
-        int grid = ctx->sm_count * occ;
+        int grid = ctx->tuning.grid_size > 0 ? ctx->tuning.grid_size : ctx->sm_count * occ;
         const unsigned long long lanes = 1ULL * grid * block;
         if (s->nphoton < lanes) grid = static_cast<int>(std::max<unsigned long long>(1ULL, (s->nphoton + block - 1) / block));
         P.aggregate = 0;
         if (ctx->tuning.budget_ms > 0) P.budget_ns = static_cast<unsigned long long>(ctx->tuning.budget_ms) * 1000000ULL;
         UMCX_CK(cudaEventRecord(ctx->ev0, st));
-        ctx->last_pack = 0;
+        ctx->last_block = block;
+        ctx->last_grid = grid;
         launch_adjoint(grid, block, smem, s->isreflect != 0, P, B, st);
         UMCX_CK(cudaGetLastError());
         UMCX_CK(cudaEventRecord(ctx->ev1, st));
@@ -851,7 +739,7 @@ void batch_enqueue(umcx_batch* b, cudaStream_t st) {
         bp.aggregate = b->tuning.aggregation == 2 ? 1 : 0;
         bp.total = ch.photons;
         bp.budget_ns = b->tuning.budget_ms > 0 ? static_cast<unsigned long long>(b->tuning.budget_ms) * 1000000ULL
-                                               : 300ULL * 1000000000ULL;
+                                               : kDefaultBudgetNs;
         KBuffers B;
         std::memset(&B, 0, sizeof(B));
         B.labels = static_cast<const uint8_t*>(b->labels.ptr);

@@ -772,6 +772,19 @@ Job make_job(const UserIO& io) {
     if (const Value* sv = session.find("RNGSeed")) rngseed = sv->as_int();
     umcx_seeds_from_rngseed(rngseed, s.seeds);
 
+    // launch shape (L739-741): when BlockSize or ThreadNum is given, CTAs of BlockSize threads (default 64) and
+    // ThreadNum / BlockSize of them (ThreadNum default 100000), as the reference's GPU build launches; the block is
+    // rounded up to whole warps because the kernels vote per warp.  Without either key the library's own
+    // persistent launch (one wave of resident CTAs) is used.
+    if (session.contains("BlockSize") || session.contains("ThreadNum")) {
+        const int64_t bs = session.value_int("BlockSize", 64), tn = session.value_int("ThreadNum", 100000);
+        if (bs < 1 || bs > 1024) throw std::runtime_error("BlockSize must be between 1 and 1024");
+        if (tn < 1) throw std::runtime_error("ThreadNum must be positive");
+        job.tuning.block_size = static_cast<int32_t>((bs + 31) / 32 * 32);
+        const int64_t grid = tn / bs;
+        job.tuning.grid_size = static_cast<int32_t>(grid < 1 ? 1 : (grid > (1 << 24) ? (1 << 24) : grid));
+    }
+
     // media table (L800-806)
     job.media.resize(static_cast<size_t>(s.mediumnum) * 4);
     for (int i = 0; i < s.mediumnum; i++) {

@@ -70,6 +70,7 @@ struct Job {
     std::vector<uint8_t> labels;  // uint8: label | 0x80 for detector voxels
     std::vector<float> media;     // [mediumnum][4], mua/mus scaled by unitinmm as at L804
     std::vector<float> detpos;    // [detnum][4]
+    umcx_tuning tuning{};         // launch shape from Session.BlockSize / ThreadNum (zeros: the library's default)
     int isnormalized = 1;
     float normalizer_for(double energytotal) const;  // L820
 };

@@ -8,8 +8,8 @@ namespace umcx_dev {
 
 template <bool R, bool D>
 static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
-    if (lc.rep == kRepWhole) k_forward<false, R, D, 0, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
-    else if (lc.rep == kRepPrefix) k_forward<false, R, D, 0, kRepPrefix><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    if (lc.rep == kRepWhole) k_forward<false, R, D, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.rep == kRepPrefix) k_forward<false, R, D, kRepPrefix><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else k_forward<false, R, D><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
 }
 
@@ -36,8 +36,8 @@ static int occ_one(int block, size_t smem) {
 template <bool R, bool D>
 static cudaError_t allow_big_smem() {
     cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D>);
-    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, 0, kRepPrefix>);
-    return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, 0, kRepWhole>) : e;
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepPrefix>);
+    return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, kRepWhole>) : e;
 }
 cudaError_t configure_fast_kernels() {
     cudaError_t e = allow_big_smem<false, false>();
@@ -54,17 +54,15 @@ int occupancy_fast(bool reflect, bool savedet, int block, size_t smem) {
 
 void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st, bool strict) {
     if (strict) launch_forward_strict(lc, P, B, st);
-    else if (lc.pack) launch_forward_packed(lc, P, B, st);
     else launch_forward_fast(lc, P, B, st);
 }
 
-size_t forward_smem(const KParams& P, int block, bool savedet, int pack) {
+size_t forward_smem(const KParams& P, int block, bool savedet) {
     size_t s = 2 * sizeof(double) * static_cast<size_t>(block);  // per-lane energy tallies
     s += sizeof(Medium) * static_cast<size_t>(P.mediumnum);
     s += sizeof(float) * static_cast<size_t>(block);  // per-lane launch weight
     if (savedet) s += sizeof(float) * static_cast<size_t>(P.ppathlen) * static_cast<size_t>(block);
     s += sizeof(float) * static_cast<size_t>(block);  // aggregation buffer
-    if (pack) s += sizeof(unsigned) * static_cast<size_t>(P.packed_words);  // packed label copy
     return s;
 }
 
@@ -80,28 +78,17 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     const bool strict = (s->flags & UMCX_SIM_STRICT_MATH) != 0;
     lc.block = t.block_size > 0 ? t.block_size : 1024;  // one CTA of 32 warps per SM: 2-3 % faster than 256
     lc.aggregate = t.aggregation == 2 ? 1 : 0;
-    lc.smem = forward_smem(P, lc.block, lc.savedet, 0);
+    lc.smem = forward_smem(P, lc.block, lc.savedet);
     while (lc.smem > kMaxDynamicSmem && lc.block > 32) {  // per-lane partial paths of many media: smaller CTAs
         lc.block /= 2;
-        lc.smem = forward_smem(P, lc.block, lc.savedet, 0);
+        lc.smem = forward_smem(P, lc.block, lc.savedet);
     }
     int occ = forward_occupancy(strict, lc.reflect, lc.savedet, lc.block, lc.smem);
     if (occ < 1) occ = 1;
-    int per_sm = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
-    // shared-memory labels only on request: measured on GB300 they run at the speed of the global-memory reads
-    // (those hit L1) and cost resident CTAs when the copy is large
-    const int bits = P.palette_bits;
-    if (!strict && bits > 0 && P.packed_words > 0 && t.label_pack == 2) {
-        const size_t smem = forward_smem(P, lc.block, lc.savedet, bits);
-        int occ_p = smem <= kMaxDynamicSmem ? occupancy_packed(lc.reflect, lc.savedet, bits, lc.block, smem) : 0;
-        const int per_sm_p = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ_p) : occ_p;
-        if (per_sm_p >= 1) {
-            lc.pack = bits;
-            lc.smem = smem;
-            per_sm = per_sm_p;
-        }
-    }
-    lc.grid = sm_count * per_sm;
+    const int per_sm = t.blocks_per_sm > 0 ? std::min(t.blocks_per_sm, occ) : occ;
+    // a requested grid (the reference's ThreadNum / BlockSize) may exceed one resident wave: the persistent CTAs
+    // of later waves start as earlier ones finish and take the photons that are left
+    lc.grid = t.grid_size > 0 ? t.grid_size : sm_count * per_sm;
     // never launch more lanes than photons need (small runs): whole warps, at least one CTA
     const unsigned long long lanes = static_cast<unsigned long long>(lc.grid) * lc.block;
     if (P.nphoton < lanes) {

@@ -28,7 +28,6 @@ struct LaunchChoice {
     size_t smem = 0;
     bool reflect = false;
     bool savedet = false;
-    int pack = 0;  // bits per voxel of the shared-memory label copy (0 = labels read from global memory)
     int rep = kRepNone;  // replication mode of the FP64 output volume (kRepPrefix / kRepWhole: KParams::rep_mask > 0)
 };
 
@@ -49,25 +48,14 @@ inline void set_extents(KBuffers& B, unsigned long long labels, unsigned long lo
 #endif
 }
 
-// dynamic shared memory of the forward kernel for a block size (pack > 0 adds the packed label copy)
-size_t forward_smem(const KParams& P, int block, bool savedet, int pack);
-
-// palette-packed labels (kernels_pack.cu): code of each label byte
-struct LabelCodes {
-    uint8_t c[256];
-};
-void launch_forward_packed(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream);
-int occupancy_packed(bool reflect, bool savedet, int pack, int block, size_t smem);
-cudaError_t configure_packed_kernels();
-void launch_label_presence(const uint8_t* labels, unsigned long long nvox, unsigned* mask, int sm_count,
-                           cudaStream_t stream);
-void launch_label_pack(const uint8_t* labels, unsigned long long nvox, int bits, const LabelCodes& codes,
-                       unsigned* words, unsigned nwords, int sm_count, cudaStream_t stream);
+// dynamic shared memory of the forward kernel for a block size
+size_t forward_smem(const KParams& P, int block, bool savedet);
 
 // resident CTAs per SM of a forward kernel instance (0 on error)
 int forward_occupancy(bool strict, bool reflect, bool savedet, int block, size_t smem);
 
-// grid = SM count x resident CTAs (persistent kernel), block size and aggregation from the tuning or defaults
+// grid = SM count x resident CTAs (persistent kernel) unless the tuning names a grid; block size and aggregation
+// from the tuning or defaults
 LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const umcx_sim* s, const KParams& P);
 
 void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream, bool strict);

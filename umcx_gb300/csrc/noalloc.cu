@@ -10,9 +10,11 @@
 // The array is a static __device__ object: every GPU that loads this library holds it (SCRATCH_BYTES) until the
 // process exits.  Host code cannot use its name as an address, so the first call on each device looks the address
 // up with cudaGetSymbolAddress (with that device current) and caches it; make that first call before any stream
-// capture.  All calls share the array and it keeps the last call's contents, so each call clears the counter and
-// tallies before its launch.  Calls whose work overlaps on the GPU (different streams, or different host threads
-// on the same device) race on the array and must be serialised by the caller.
+// capture.  The cached address belongs to the device's primary context: after a cudaDeviceReset by the host
+// application the entry point must not be called again in that process.  Every call synchronises its stream before
+// it returns (it reads the tallies back).  All calls share the array and it keeps the last call's contents, so
+// each call clears the counter and tallies before its launch.  Calls whose work overlaps on the GPU (different
+// streams, or different host threads on the same device) race on the array and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -21,6 +23,7 @@
 
 #include "../../include/umcx_gpu.h"
 #include "launch.h"
+#include "params.h"
 #include "propagate.cuh"
 
 using namespace umcx_dev;
@@ -69,17 +72,10 @@ extern "C" int umcx_gpu_forward_noalloc(int device, const umcx_sim* s, const uin
                                         umcx_result* res) {
     const auto t0 = std::chrono::steady_clock::now();
     if (res) std::memset(res, 0, sizeof(*res));
-    if (!s || !d_labels || !media || (s->detnum > 0 && !detpos)) return fail(res, UMCX_ERR_INPUT);
-    if (s->flags & ~UMCX_SIM_FLAGS_ALL) return fail(res, UMCX_ERR_INPUT);
-    for (int k = 0; k < 3; k++)
-        if (s->dim[k] < 1 || s->dim[k] > 32767) return fail(res, UMCX_ERR_INPUT);
-    if (s->dim[3] < 1 || s->dim[3] > UMCX_MAX_GATES) return fail(res, UMCX_ERR_INPUT);
+    // the same input rules as every other entry point (params.h), plus the optical table's fit in the fixed array
+    if (check_sim(s) || !d_labels || !media || (s->detnum > 0 && !detpos)) return fail(res, UMCX_ERR_INPUT);
+    if (s->mediumnum > UMCX_NOALLOC_MAX_MEDIA) return fail(res, UMCX_ERR_INPUT);
     const unsigned long long nout = 1ULL * s->dim[0] * s->dim[1] * s->dim[2] * s->dim[3];
-    if (nout >= (1ULL << 31)) return fail(res, UMCX_ERR_INPUT);
-    // the optical table must fit the fixed scratch array
-    if (s->mediumnum < 1 || s->mediumnum > UMCX_NOALLOC_MAX_MEDIA) return fail(res, UMCX_ERR_INPUT);
-    if (s->detnum < 0 || s->detnum > UMCX_MAX_DET) return fail(res, UMCX_ERR_INPUT);
-    if (s->srctype < 0 || s->srctype > 6 || !(s->rtstep > 0.f)) return fail(res, UMCX_ERR_INPUT);
     if (s->issavevol && !d_fluence) return fail(res, UMCX_ERR_INPUT);
     if (s->issavedet && s->maxdetphotons > 0 && !d_detp) return fail(res, UMCX_ERR_INPUT);
     int ndev = 0;
@@ -93,50 +89,10 @@ extern "C" int umcx_gpu_forward_noalloc(int device, const umcx_sim* s, const uin
         return fail(res, UMCX_ERR_CUDA);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-    // kernel parameters and the optical table (same derived constants as the allocating entry points)
-    KParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.nx = static_cast<int>(s->dim[0]);
-    P.ny = static_cast<int>(s->dim[1]);
-    P.nz = static_cast<int>(s->dim[2]);
-    P.maxgate = static_cast<int>(s->dim[3]);
-    P.dimyz = s->dim[1] * s->dim[2];
-    P.dimxyz = P.dimyz * s->dim[0];
-    P.nphoton = s->nphoton;
-    P.photon_offset = s->photon_offset;
-    P.tstart = s->tstart;
-    P.tend = s->tend;
-    P.rtstep = s->rtstep;
-    P.unitinmm = s->unitinmm;
-    P.isreflect = s->isreflect;
-    P.issavevol = s->issavevol;
-    P.issavedet = s->issavedet;
-    P.savedetflag = s->savedetflag;
-    P.mediumnum = s->mediumnum;
-    P.outputtype = s->outputtype;
-    P.detnum = s->detnum;
-    P.srctype = s->srctype;
-    P.maxdetphotons = s->issavedet ? s->maxdetphotons : 0u;
-    P.cols = umcx_detp_columns(s);
-    P.ppathlen = (s->issavedet && (s->savedetflag & UMCX_DET_PPATH)) ? s->mediumnum : 0;
-    P.step_cap = kDefaultStepCap;
-    for (int k = 0; k < 4; k++) P.seeds[k] = s->seeds[k];
-    P.srcpos = make_float4(s->srcpos[0], s->srcpos[1], s->srcpos[2], 1.f);
-    P.srcdir = make_float4(s->srcdir[0], s->srcdir[1], s->srcdir[2], 0.f);
-    P.srcrdir = make_float4(1.f / s->srcdir[0], 1.f / s->srcdir[1], 1.f / s->srcdir[2], 0.f);
-    P.srcparam1 = make_float4(s->srcparam1[0], s->srcparam1[1], s->srcparam1[2], s->srcparam1[3]);
-    P.srcparam2 = make_float4(s->srcparam2[0], s->srcparam2[1], s->srcparam2[2], s->srcparam2[3]);
-    P.budget_ns = 600ULL * 1000000000ULL;
-    for (int d = 0; d < s->detnum; d++)
-        P.det[d] = make_float4(detpos[4 * d], detpos[4 * d + 1], detpos[4 * d + 2], detpos[4 * d + 3]);
+    // kernel parameters and the optical table: the helpers the allocating entry points use
+    KParams P = make_params(s, detpos);
     Medium hm[UMCX_NOALLOC_MAX_MEDIA];
-    for (int i = 0; i < s->mediumnum; i++) {
-        const float mua = media[4 * i], mus = media[4 * i + 1], g = media[4 * i + 2], n = media[4 * i + 3];
-        hm[i].a = make_float4(mua, mus, g, n);
-        hm[i].b = make_float4(mus != 0.f ? 1.f / mus : 0.f, deposit_factor(mua, s->outputtype),
-                              g != 0.f ? 1.f / (2.f * g) : 0.f, n * kOneOverC0);
-        hm[i].c = make_float4(1.f - g * g, 1.f - g, 2.f * g, 1.f + g * g);
-    }
+    for (int i = 0; i < s->mediumnum; i++) hm[i] = make_medium(media + 4 * i, s->outputtype);
 
     KBuffers B;
     std::memset(&B, 0, sizeof(B));
@@ -184,6 +140,8 @@ extern "C" int umcx_gpu_forward_noalloc(int device, const umcx_sim* s, const uin
         res->kernel_ms = 0.f;  // no CUDA events are created on this path
         res->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
         res->status = rc;
+        res->block_size = lc.block;
+        res->grid_size = lc.grid;
     }
     return rc;
 }

@@ -97,9 +97,6 @@ struct KParams {
     unsigned seeds[4];
     float4 srcpos, srcdir, srcrdir, srcparam1, srcparam2;
     unsigned long long budget_ns;  // wall-clock budget of the launch (checked against %globaltimer)
-    unsigned palette[4];           // palette-packed labels: label byte of each code (4 bytes per word)
-    unsigned packed_words;         // words of the packed label volume, a multiple of 4 (0 = not packed)
-    int palette_bits;              // bits per voxel of the packed volume (2 or 4; 0 = not packed)
     unsigned rep_mask;             // forward kernel: CTA b deposits into copy c = b & rep_mask of the first rep_len
     unsigned rep_len;              // elements of the FP64 volume (copy 0 is the volume itself; see accumulator_replicas)
     float4 det[UMCX_MAX_DET];
@@ -119,7 +116,6 @@ constexpr int kCheckError = 16;
 
 struct KBuffers {
     const uint8_t* labels;
-    const unsigned* packed;  // palette-packed labels (16-byte aligned, padded to whole uint4)
     float* fluence;
     double* fluence64;   // optional FP64 accumulation volume (same layout as fluence)
     float* detp;
@@ -652,9 +648,7 @@ struct Event {
     unsigned scat_mid;
 };
 
-// Label sources.  GlobalLabels reads the uint8 volume through the read-only path; PackedLabels reads a palette-
-// packed copy (BITS per voxel, 32/BITS voxels per 32-bit word) held in shared memory, with the palette (up to 16
-// label bytes) in registers.
+// Label source of the propagation loop: the uint8 volume read through the read-only path.
 struct GlobalLabels {
     const uint8_t* __restrict__ p;
 #if UMCX_DEVICE_CHECKS
@@ -687,21 +681,6 @@ __device__ __forceinline__ GlobalLabels global_labels(const KBuffers& B, unsigne
 #endif
     return g;
 }
-
-template <int BITS>
-struct PackedLabels {
-    const unsigned* words;  // shared memory
-    uint4 pal;              // palette: byte k of the 16 is the label byte of code k
-    __device__ __forceinline__ unsigned operator()(int i) const {
-        constexpr int kPer = 32 / BITS;
-        constexpr int kShift = BITS == 2 ? 4 : 3;
-        const unsigned code = (words[i >> kShift] >> ((i & (kPer - 1)) * BITS)) & ((1u << BITS) - 1u);
-        if (BITS == 2) return (pal.x >> (code * 8u)) & 0xFFu;
-        const unsigned q = code >> 2;
-        const unsigned w = q == 0 ? pal.x : (q == 1 ? pal.y : (q == 2 ? pal.z : pal.w));
-        return (w >> ((code & 3u) * 8u)) & 0xFFu;
-    }
-};
 
 // the kernels call this where a photon ends: photons stopped by the step cap or the zero-progress guard
 __device__ __forceinline__ void count_stopped(const Photon& p) {
@@ -951,17 +930,8 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
 }
 
 // =============================================================================================== forward kernel
-// Shared memory: Medium[mediumnum] | float ppath[ppathlen][blockDim] | float aggbuf[blockDim]
-template <int PACK>
-struct LabelViewOf {
-    using type = PackedLabels<PACK>;
-};
-template <>
-struct LabelViewOf<0> {
-    using type = GlobalLabels;
-};
-
-// PACK = 0 reads labels from global memory; PACK = 2 or 4 reads the palette-packed copy staged in shared memory
+// Shared memory: double tally[2][blockDim] | Medium[mediumnum] | float ppath[ppathlen][blockDim] |
+// float aggbuf[blockDim] | float launch weight[blockDim]
 // launch bounds of the forward kernel (a build variant can trade resident lanes for registers, e.g.
 // UMCX_NVCC_DEFS="UMCX_FWD_THREADS=256 UMCX_FWD_MINB=3"; measured on GB300 the default 1024 x 1 at 64 registers is
 // as fast as 768 lanes at 74 registers and faster than 512 lanes at 86)
@@ -970,7 +940,7 @@ struct LabelViewOf<0> {
 #define UMCX_FWD_MINB 1
 #endif
 // REP: replication mode of the FP64 output volume (P.rep_mask, P.rep_len; see accumulator_replicas)
-template <bool STRICT, bool REFLECT, bool SAVEDET, int PACK = 0, int REP = kRepNone>
+template <bool STRICT, bool REFLECT, bool SAVEDET, int REP = kRepNone>
 __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
@@ -980,17 +950,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
     float* ppath = reinterpret_cast<float*>(sm + P.mediumnum);
     float* aggbuf = ppath + (SAVEDET ? P.ppathlen * blockDim.x : 0);
     float* lwbuf = aggbuf + blockDim.x;
-    unsigned* lwords = reinterpret_cast<unsigned*>(lwbuf + blockDim.x);
-    typename LabelViewOf<PACK>::type labels;
-    if constexpr (PACK == 0) {
-        labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
-    } else {
-        const uint4* src = reinterpret_cast<const uint4*>(B.packed);
-        uint4* dst = reinterpret_cast<uint4*>(lwords);
-        for (unsigned k = threadIdx.x; k < (P.packed_words + 3u) / 4u; k += blockDim.x) dst[k] = src[k];
-        labels.words = lwords;
-        labels.pal = make_uint4(P.palette[0], P.palette[1], P.palette[2], P.palette[3]);
-    }
+    const GlobalLabels labels = global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum));
     load_media(P, B.media, sm);
 
     const unsigned tid = threadIdx.x;

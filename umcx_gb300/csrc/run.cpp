@@ -53,6 +53,8 @@ int run_simulation(int argc, const char* const argv[], std::string* errmsg) {
         int rc = umcx_create(&ctx, device_from(io));
         if (rc != UMCX_OK) throw std::runtime_error("no usable CUDA device for the simulation");
         std::unique_ptr<umcx_context, void (*)(umcx_context*)> guard(ctx, umcx_destroy);
+        if ((job.tuning.block_size || job.tuning.grid_size) && umcx_set_tuning(ctx, &job.tuning) != UMCX_OK)
+            throw std::runtime_error(std::string("invalid launch shape: ") + umcx_last_error(ctx));
 
         const auto t0 = std::chrono::steady_clock::now();  // MCX_clock at L812 (includes transfers)
         const size_t nout = 1ULL * s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3];
@@ -176,6 +178,11 @@ int umcx_job_build_labels(const umcx_job* j, umcx_context* ctx, uint8_t* d_label
     dom.detpos = j->job.detpos.data();
     dom.detnum = j->job.sim.detnum;
     return umcx_gpu_build_labels(ctx, &dom, d_labels);
+}
+int umcx_job_tuning(const umcx_job* j, umcx_tuning* out) {
+    if (!j || !j->io || !out) return UMCX_ERR_INPUT;
+    *out = j->job.tuning;
+    return UMCX_OK;
 }
 const float* umcx_job_media(const umcx_job* j) { return j ? j->job.media.data() : nullptr; }
 const float* umcx_job_detpos(const umcx_job* j) { return j ? j->job.detpos.data() : nullptr; }
