@@ -34,6 +34,7 @@ FAST = ["--use_fast_math"]
 CU_UNITS = {
     "capi.cu": [],
     "kernels_fast.cu": FAST,
+    "kernels_fast_agg.cu": FAST,
     "kernels_strict.cu": ["--fmad=false"],
     "kernels_adjoint.cu": FAST,
     "kernels_batch.cu": FAST,

@@ -14,6 +14,10 @@ static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers&
 }
 
 void launch_forward_fast(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
+    if (lc.aggregate) {
+        launch_forward_fast_agg(lc, P, B, st);
+        return;
+    }
     if (lc.reflect) {
         if (lc.savedet) launch_one<true, true>(lc, P, B, st);
         else launch_one<true, false>(lc, P, B, st);
@@ -40,7 +44,8 @@ static cudaError_t allow_big_smem() {
     return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, kRepWhole>) : e;
 }
 cudaError_t configure_fast_kernels() {
-    cudaError_t e = allow_big_smem<false, false>();
+    cudaError_t e = configure_fast_agg_kernels();
+    if (e == cudaSuccess) e = allow_big_smem<false, false>();
     if (e == cudaSuccess) e = allow_big_smem<false, true>();
     if (e == cudaSuccess) e = allow_big_smem<true, false>();
     if (e == cudaSuccess) e = allow_big_smem<true, true>();

@@ -60,6 +60,9 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
 
 void launch_forward(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream, bool strict);
 void launch_forward_fast(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream);
+// instances with warp-aggregated fluence deposits (kernels_fast_agg.cu)
+void launch_forward_fast_agg(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream);
+cudaError_t configure_fast_agg_kernels();
 void launch_forward_strict(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t stream);
 int occupancy_fast(bool reflect, bool savedet, int block, size_t smem);
 cudaError_t configure_fast_kernels();

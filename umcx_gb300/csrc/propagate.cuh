@@ -459,7 +459,7 @@ __device__ __forceinline__ void scatter(Photon& p, const Medium& m) {
         ctheta = fabsf(g) > FLT_EPSILON ? (m.c.w - t * t) * m.b.z : 2.f * r - 1.f;
         ctheta = fmaxf(-1.f, fminf(1.f, ctheta));
         const float s2 = fmaxf(0.f, 1.f - ctheta * ctheta);
-        stheta = s2 > 0.f ? s2 * rsqrtf(s2) : 0.f;
+        stheta = sqrtf(s2);
     }
     rotate<STRICT>(p, stheta, ctheta, sphi, cphi);
     p.rx = rcp_<STRICT>(p.vx);
@@ -592,7 +592,7 @@ __device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v,
     if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), UMCX_EXTENT(B, n_out),
                   kSiteOutput))
         return;
-    if (B.fluence64) {
+    if (REP != kRepNone || B.fluence64) {  // a replicated volume is always the FP64 accumulator
         if (REP == kRepNone) {
             atomicAdd(B.fluence64 + idx, static_cast<double>(v));
         } else {  // 32-bit element offsets (idx >= 0 here)
@@ -929,6 +929,69 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
     return false;
 }
 
+// One iteration of the forward kernel for an active photon with plain fluence atomics: advance() with the
+// partial-path update (L286-288) and the deposit (L289-291, L359-363) made where the voxel crossing is handled, so
+// that neither the deposit's address and value nor the crossing's bookkeeping stay live through the scattering code.
+// Returns true when the photon ended.  (The warp-aggregated mode deposits after the divergent part instead: its
+// __match_any_sync needs the whole warp.)
+template <bool STRICT, bool REFLECT, bool SAVEDET, int REP, class LV>
+__device__ __forceinline__ bool forward_step(const KParams& P, const KBuffers& B, const LV& labels, const Medium* sm,
+                                             Photon& p, Counters& c, float* ppath_lane, const Replica& rep) {
+    bool term = false;
+    if (p.lx > 0.f) {
+        const unsigned mid = p.media & UMCX_LABEL_MASK;
+        const Medium m = sm[mid];
+        bool crossed;
+        float moved;
+        int newvox = step<STRICT>(P, p, m, &crossed, &moved);
+        // (the lane's step count is taken from p.nsteps when the photon ends)
+        // zero-progress guard and step cap, as in advance()
+        if (moved == 0.f) p.media += 0x10000u;
+        else p.media &= 0xFFFFu;
+        const bool capped = ++p.nsteps > P.step_cap || p.media >= (kZeroStepLimit << 16);
+        p.media |= capped ? kStoppedBit : 0u;
+        term = capped;
+        if (!capped && newvox != p.lastvox) {
+            c.cross++;
+            // the next voxel's label first: its load overlaps the deposit below
+            const bool late = p.ly > P.tend;
+            unsigned newmedia = (newvox >= 0 && !late) ? labels(newvox) : 0u;
+            if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && mid > 0 &&
+                index_ok(&B.stats->error, mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
+                ppath_lane[(mid - 1) * blockDim.x] += p.lz;
+            if (P.issavevol) {
+                const int gate = min(__float2int_rd((p.ly - P.tstart) * P.rtstep), P.maxgate - 1);
+                if (gate >= 0)
+                    deposit_add<REP>(B, p.lastvox + gate * static_cast<int>(P.dimxyz), deposit_value<STRICT>(P, p, m),
+                                     rep);
+                p.lw = p.pw;
+                p.lz = 0.f;
+            }
+            const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
+            term = late || newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0);
+            if (REFLECT && !late && m.a.w != n2) {
+                rare_count(kRareRefl);
+                if (reflect<STRICT>(p, m.a.w, n2)) {
+                    term = newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0;
+                } else {
+                    term = false;
+                    newvox = p.lastvox;
+                    newmedia = p.media;
+                }
+            }
+            if (!term) {
+                p.lastvox = newvox;
+                p.media = newmedia;
+            }
+        }
+    }
+    if (!term && p.lx <= 0.f) {
+        scatter<STRICT>(p, sm[p.media & UMCX_LABEL_MASK]);
+        c.scat++;
+    }
+    return term;
+}
+
 // =============================================================================================== forward kernel
 // Shared memory: double tally[2][blockDim] | Medium[mediumnum] | float ppath[ppathlen][blockDim] |
 // float aggbuf[blockDim] | float launch weight[blockDim]
@@ -939,8 +1002,9 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
 #define UMCX_FWD_THREADS 1024
 #define UMCX_FWD_MINB 1
 #endif
-// REP: replication mode of the FP64 output volume (P.rep_mask, P.rep_len; see accumulator_replicas)
-template <bool STRICT, bool REFLECT, bool SAVEDET, int REP = kRepNone>
+// REP: replication mode of the FP64 output volume (P.rep_mask, P.rep_len; see accumulator_replicas); AGG: fluence
+// deposits aggregated per warp with __match_any_sync (P.aggregate) instead of plain atomics
+template <bool STRICT, bool REFLECT, bool SAVEDET, int REP = kRepNone, bool AGG = false>
 __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
@@ -986,17 +1050,24 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
             if (out_of_budget(B, iter, lane)) break;
         }
 
-        Event ev;
-        advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c, active);  // no event on an idle lane
-        if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0 &&
-            index_ok(&B.stats->error, ev.left_mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
-            ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
-        const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
-        const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
-        const float dep_val = dep ? ev.dep_val : 0.f;
-        deposit_converged<REP>(B, P.aggregate != 0, aggbuf, tid, lane, dep_idx, dep_val, replica);
-        if (ev.term) {
+        bool term = false;
+        if (AGG) {
+            Event ev;
+            advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c, active);  // no event on an idle lane
+            if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0 &&
+                index_ok(&B.stats->error, ev.left_mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
+                ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
+            const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
+            const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
+            const float dep_val = dep ? ev.dep_val : 0.f;
+            deposit_converged<REP>(B, true, aggbuf, tid, lane, dep_idx, dep_val, replica);
+            term = ev.term;
+        } else if (active) {
+            term = forward_step<STRICT, REFLECT, SAVEDET, REP>(P, B, labels, sm, p, c, ppath + tid, replica);
+        }
+        if (term) {
             count_stopped(p);
+            if (!AGG) c.steps += p.nsteps;  // forward_step does not count steps one by one
             if (SAVEDET) {
                 const bool tdet = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
                 append_detected(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
