@@ -1,18 +1,26 @@
 """Benchmark of the umcx photon-transport hot path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--photons P]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--photons P] [--forms LIST]
 
-Workload: the heterogeneous forward configuration with refractive mismatch and detectors -- 60x60x60 voxels of
-1 mm, background label 1 (mua 0.005/mm, mus 1/mm, g 0.01, n 1.37), a radius-15 sphere of label 2 (mua 0.002,
-mus 5, g 0.9, n 1.0) centred at (30,30,30), pencil source at (29,29,0) along +z, boundary reflection on, 1e7
-photons per step, 50 time gates over 0-5 ns, four disk detectors of radius 1 mm at z = 0 with partial
-pathlengths saved.  Synthetic input (the configuration is generated, not read from a dataset).
+Headline workload (configuration 2): the heterogeneous forward configuration with refractive mismatch and
+detectors -- 60x60x60 voxels of 1 mm, background label 1 (mua 0.005/mm, mus 1/mm, g 0.01, n 1.37), a radius-15
+sphere of label 2 (mua 0.002, mus 5, g 0.9, n 1.0) centred at (30,30,30), pencil source at (29,29,0) along +z,
+boundary reflection on, 1e7 photons per step, 50 time gates over 0-5 ns, four disk detectors of radius 1 mm at
+z = 0 with partial pathlengths saved.  Synthetic input (the configuration is generated, not read from a dataset).
 
 One step = one full simulation of P photons.  `value` is photons/ms of the propagation kernel with the inputs
-resident in HBM (CUDA events on the launching stream; the fluence output, 43 MB, is cleared inside the step and the
-L2 is flushed by writing a 256 MB buffer between steps).  `e2e` is the same metric through the C ABI call with host
+resident in HBM (CUDA events on the launching stream; the output volume is cleared inside the step and the L2 is
+flushed by writing a 256 MB buffer between steps).  `e2e` is the same metric through the C ABI call with host
 buffers in page-locked memory (umcx_gpu_forward: label upload, simulation, fluence + detected-photon download),
-timed on the host.
+timed on the host.  Under torchrun (N > 1) every rank simulates its own photon range of one N x P-photon
+simulation and the ranks sum the output volume and the tallies on the GPU and gather the detected rows inside the
+timed step (umcx_gb300.shard): weak scaling.
+
+`forms` (rank 0, N = 1 sizes) measures the other configurations the same way, each with its device time, end-to-end
+time and roofline fractions: configuration 1 at its 1e6 photons, the reference's own published benchmark cube60
+(configuration 1 plus four saved detectors, 1e8 photons), configuration 3 at 1e8 photons, the forward + adjoint form
+(configuration 4) and the batched form (configuration 5, 256 simulations at their full photon budgets, against the
+same simulations as sequential single launches).
 
 --impl reference times the reference's own CPU implementation (the unmodified reference program built from its
 sources, oracle/_ref/umcx, with all host threads; else the C restatement in oracle/) on a bounded photon sample of
@@ -34,32 +42,30 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-CONFIG = {
-    "Session": {"ID": "bench_c2", "Photons": 10000000, "RNGSeed": 1648335518, "DoMismatch": 1, "DoPartialPath": 1,
-                "SaveDetFlag": 5, "OutputType": "x"},
-    "Forward": {"T0": 0, "T1": 5e-9, "Dt": 1e-10},
-    "Domain": {"Dim": [60, 60, 60], "LengthUnit": 1,
-               "Media": [{"mua": 0, "mus": 0, "g": 1, "n": 1}, {"mua": 0.005, "mus": 1.0, "g": 0.01, "n": 1.37},
-                         {"mua": 0.002, "mus": 5.0, "g": 0.9, "n": 1.0}]},
-    "Optode": {"Source": {"Type": "pencil", "Pos": [29, 29, 0], "Dir": [0, 0, 1]},
-               "Detector": [{"Pos": [29, 19, 0], "R": 1}, {"Pos": [19, 29, 0], "R": 1},
-                            {"Pos": [29, 39, 0], "R": 1}, {"Pos": [39, 29, 0], "R": 1}]},
-    "Shapes": [{"Grid": {"Tag": 1, "Size": [60, 60, 60]}}, {"Sphere": {"O": [30, 30, 30], "R": 15, "Tag": 2}}],
-}
+from umcx_gb300.workloads import config1, config2, config3  # noqa: E402
+
+CONFIG = config2()
 WORKLOAD = "heterogeneous forward, 60^3 grid, sphere R15, reflection on, 50 gates, 4 detectors (ppath saved)"
 METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates, 4 detectors)"
 
-# DRAM bytes (read + write) of one propagation launch of the default workload (1e7 photons), from an ncu capture
-# of the same command (dram__bytes_read.sum + dram__bytes_write.sum: 93.5 MB of label and table reads, 3.06 GB of
-# FP64-accumulator lines, the volume and the copies of its first gates, written back as L2 evicts them); not
-# measured live, reported only for the default size
-DRAM_BYTES_DEFAULT_LAUNCH = 93_477_376 + 3_064_464_000
-
-# warp instructions issued per voxel step by the propagation kernel, from an ncu capture of the default launch
-# (smsp__inst_executed.sum 4.37e10 over 3.436e9 steps; block 1024, plain atomics), captured before the copies of
-# the output volume took 32-bit offsets (a few instructions fewer per deposit, so a slight overestimate); with the
-# live step count and kernel time it gives the issue rate against the SMs' 4 issue slots per cycle
-WARP_INST_PER_STEP = 12.72
+# per workload: the input, its photons per step, timed steps of a `forms` entry, and what an ncu capture of the
+# propagation kernel on the same build measured (profiles/): warp instructions issued per voxel step
+# (smsp__inst_executed.sum / steps) and DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch at
+# that photon count.  None where no capture exists; the line then reports null for those fractions.
+FORWARD = {
+    "c2": {"json": CONFIG, "photons": 10000000, "workload": WORKLOAD,
+           "warp_inst_per_step": None, "dram_bytes": None},
+    "c1": {"json": config1(), "photons": 1000000, "steps": 20,
+           "workload": "homogeneous 60^3 cube, pencil beam, one 5 ns gate, no reflection (configuration 1)",
+           "warp_inst_per_step": None, "dram_bytes": None},
+    "cube60": {"args": ["--bench", "cube60"], "photons": 100000000, "steps": 5,
+               "workload": "the reference's cube60 benchmark: configuration 1 plus four saved detectors, 1e8 photons "
+                           "(published: 175 075 photons/ms on an RTX 5090)",
+               "warp_inst_per_step": None, "dram_bytes": None},
+    "c3": {"json": config3(), "photons": 100000000, "steps": 5,
+           "workload": "200^3 layered domain of 0.005 mm voxels with a cylinder, disk source, 1 ns gate (configuration 3)",
+           "warp_inst_per_step": None, "dram_bytes": None},
+}
 
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
 # step L316-337, scatter L364-380, voxel crossing / deposit L285-310, reflect L381-417
@@ -180,6 +186,10 @@ def run_reference_arm(args) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (generated configuration)",
         "config": {"workload": WORKLOAD, "photons_per_step": photons, "threads": threads,
+                   "photons_per_step_of_the_gpu_arm": int(CONFIG["Session"]["Photons"]),
+                   "sample": "a bounded sample of the same simulation per step: at the CPU's rate the GPU arm's "
+                             "1e7 photons would take about 15 s per step; photons/ms does not depend on the count "
+                             "(1e6 photons gave the same rate)",
                    "program": "reference umcx CPU OpenMP build" if info["kind"] == "reference" else "oracle C port"},
         "cpu_baseline": {"value": value, "unit": "photons/ms", "cores": threads, "kind": info["kind"],
                          "sample": f"{photons} photons of the benchmark configuration per step"},
@@ -188,6 +198,144 @@ def run_reference_arm(args) -> None:
         "absorbed_percent": info["absorbed"], "detected": info["detected"],
     }
     print(json.dumps(line), flush=True)
+
+
+def job_of(spec: dict, photons: int):
+    from umcx_gb300 import Job
+
+    if "json" in spec:
+        cfg = json.loads(json.dumps(spec["json"]))
+        cfg["Session"]["Photons"] = int(photons)
+        return Job.from_json(cfg)
+    return Job.from_args([*spec["args"], "-n", str(int(photons))])
+
+
+def roofline(r, kms: float, peaks: dict, hbm_peak: float, spec: dict) -> dict:
+    """Fractions of the propagation kernel: the formula FP32 operations (per-event counts x the launch's events)
+    against the live FMA rate and against SMs x 128 lanes x clock; SFU operations; fluence atomics against the
+    scattered-atomic rate; warp instructions issued (ncu count per step x live steps) against 4 issue slots per SM
+    and cycle; algorithmic bytes against HBM."""
+    fp32_ops = sum(getattr(r, k) * v for k, v in OPS_FP32.items())
+    sfu_ops = sum(getattr(r, k) * v for k, v in OPS_SFU.items())
+    sec = kms * 1e-3
+    achieved = fp32_ops / sec / 1e12
+    peak = peaks["fp32_fma_per_s"] / 1e12
+    spec_peak = peaks["sm_count"] * 128 * peaks["sm_clock_khz"] * 1e3 / 1e12
+    issue_peak = peaks["sm_count"] * 4 * peaks["sm_clock_khz"] * 1e3
+    wips = spec.get("warp_inst_per_step")
+    issue = None
+    if wips:
+        issue = {"achieved_warp_inst_per_s": r.steps * wips / sec, "peak_warp_inst_per_s": issue_peak,
+                 "frac": r.steps * wips / sec / issue_peak, "warp_inst_per_step": wips,
+                 "source": "instructions per step from an ncu capture of this build (profiles/)"}
+    return {"bound": "fp32", "achieved": achieved, "peak": peak,
+            "unit": "Top/s (FP32 instructions, FMA = 1 op; peak measured live by an FMA loop)",
+            "frac": achieved / peak,
+            "frac_of_spec_rate": achieved / spec_peak, "spec_rate": spec_peak,
+            "traffic": spec.get("dram_bytes"),
+            "ops_per_launch": fp32_ops,
+            "events_per_launch": {k: int(getattr(r, k)) for k in OPS_FP32},
+            "sfu": {"achieved": sfu_ops / sec / 1e12, "peak": peaks["sfu_per_s"] / 1e12,
+                    "frac": sfu_ops / sec / peaks["sfu_per_s"], "unit": "Top/s"},
+            "l2_atomics": {"achieved_per_s": r.crossings / sec, "peak_per_s": peaks["l2_atomic_per_s"],
+                           "frac": r.crossings / sec / peaks["l2_atomic_per_s"]},
+            "hbm": {"algorithmic_gbs": r.crossings * 9.0 / sec / 1e9, "peak_gbs": hbm_peak},
+            "issue": issue}
+
+
+def time_forward(ctx, job, photons: int, steps: int, warmup: int, device: int, flush, shard=None):
+    """Device-timed steps (kernel + output rounding; plus, with a shard, the cross-rank reduction) and the results."""
+    import torch
+
+    from umcx_gb300 import detp_columns
+
+    sim = job.sim
+    if shard is not None:
+        sim.photon_offset, sim.nphoton = shard.photon_range(photons)
+    nvox = sim.dim[0] * sim.dim[1] * sim.dim[2]
+    nout = nvox * sim.dim[3]
+    d_lab = torch.from_numpy(job.labels.ravel().copy()).to(f"cuda:{device}")
+    d_flu = torch.empty(nout, dtype=torch.float32, device=f"cuda:{device}")
+    d_det = torch.empty(max(1, sim.maxdetphotons * detp_columns(sim)), dtype=torch.float32, device=f"cuda:{device}")
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        ctx.forward_device(sim, d_lab, job.media, job.detpos, d_flu, d_det, stream)
+    step_ms, kernel_ms, results = [], [], []
+    if shard is not None:
+        shard.barrier()
+    torch.cuda.synchronize()
+    for _ in range(steps):
+        flush.fill_(1)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        r = ctx.forward_device(sim, d_lab, job.media, job.detpos, d_flu, d_det, stream)
+        if shard is not None:
+            shard.reduce_device(d_flu, d_det[: r.saved * detp_columns(sim)].view(-1, detp_columns(sim))
+                                if sim.issavedet and detp_columns(sim) else None, r)
+        ev1.record(stream)
+        ev1.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+        kernel_ms.append(r.kernel_ms)
+        results.append(r)
+    if shard is not None:
+        shard.barrier()
+    torch.cuda.synchronize()
+    return step_ms, kernel_ms, results
+
+
+def time_e2e(ctx, job, photons: int, reps: int, flush) -> dict:
+    """photons/ms through umcx_gpu_forward with host buffers (caller-owned, page-locked, reused)."""
+    import torch
+
+    from umcx_gb300 import detp_columns
+
+    sim = job.sim
+    nvox = sim.dim[0] * sim.dim[1] * sim.dim[2]
+    nout = nvox * sim.dim[3]
+
+    def pinned(n, dtype):
+        return torch.ones(n, dtype=dtype, pin_memory=True).numpy()
+
+    h_lab = pinned(nvox, torch.uint8)
+    h_lab[:] = job.labels.reshape(-1)
+    h_flu = pinned(nout, torch.float32) if sim.issavevol else None
+    h_dp = pinned(max(1, sim.maxdetphotons * detp_columns(sim)), torch.float32) if sim.issavedet else None
+    ms = []
+    for _ in range(max(1, reps)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = ctx.forward(sim, h_lab, job.media, job.detpos, fluence=h_flu, detp=h_dp)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    r = out.result
+    h2d = nvox + 4 * 4 * sim.mediumnum + 4 * 4 * sim.detnum
+    d2h = (nout * 4 if sim.issavevol else 0) + int(r.saved) * detp_columns(sim) * 4 + 96
+    m = statistics.mean(ms)
+    return {"value": photons / m, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": m}
+
+
+def measure_form(ctx, name: str, args, device: int, flush, peaks: dict, hbm_peak: float) -> dict:
+    """One single-simulation configuration: device-timed photons/ms, end-to-end photons/ms, roofline fractions."""
+    from umcx_gb300._lib import SIM_FP32_ACCUM
+
+    spec = FORWARD[name]
+    photons = int(spec["photons"])
+    job = job_of(spec, photons)
+    steps = spec.get("steps", 10)
+    step_ms, kernel_ms, results = time_forward(ctx, job, photons, steps, 3, device, flush)
+    r = results[-1]
+    kms = statistics.mean(kernel_ms)
+    launches_per_step = 2 if (job.sim.issavevol and not (job.sim.flags & SIM_FP32_ACCUM)) else 1
+    return {"workload": spec["workload"], "photons": photons, "steps": steps,
+            "photons_per_ms": photons * steps / sum(step_ms), "ms_per_step": sum(step_ms) / steps, "kernel_ms": kms,
+            "e2e": time_e2e(ctx, job_of(spec, photons), photons, 3, flush),
+            "gpu_launches_per_step": launches_per_step,
+            "roofline": roofline(r, kms, peaks, hbm_peak, spec),
+            "physics": {"absorbed_percent": (r.energy_total - r.energy_escape) / r.energy_total * 100,
+                        "detected": int(r.detected), "steps_per_photon": r.steps / r.launched,
+                        "scatters_per_photon": r.scatters / r.launched}}
 
 
 def measure_adjoint(ctx, args) -> dict:
@@ -241,7 +389,7 @@ def measure_batched(ctx, args, device) -> dict:
     if args.no_autotune:
         tune = {"block_size": 1024, "blocks_per_sm": 0, "aggregation": 1, "source": "fixed"}
     else:
-        tune = autotune_batch(ctx, jobs, fraction=0.2, min_photons=500,
+        tune = autotune_batch(ctx, jobs, fraction=0.1 if args.batch_scale >= 0.5 else 0.2, min_photons=500,
                               candidates=((512, 1), (1024, 1), (512, 2), (1024, 2)))
     b.set_tuning(tune["block_size"], tune["blocks_per_sm"], tune["aggregation"])
     b.run()
@@ -283,164 +431,101 @@ def measure_batched(ctx, args, device) -> dict:
 
 
 def run_gpu_arm(args) -> None:
-    import numpy as np
     import torch
 
-    from umcx_gb300 import Context, Job, detp_columns, measure_peaks
+    from umcx_gb300 import Context, measure_peaks
     from umcx_gb300._lib import SIM_FP32_ACCUM
 
     ws, rank, local = dist_env()
+    shard = None
     if ws > 1:
-        import torch.distributed as dist
+        from umcx_gb300.shard import Shard
 
         torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        shard = Shard.init("nccl")
     device = local if ws > 1 else 0
     torch.cuda.set_device(device)
 
-    cfg = json.loads(json.dumps(CONFIG))
-    cfg["Session"]["Photons"] = int(args.photons)
-    job = Job.from_json(cfg)
-    sim = job.sim
-    sim.photon_offset = rank * int(args.photons)  # weak scaling: each rank simulates its own photon range
+    spec = FORWARD["c2"]
+    photons = int(args.photons)
+    job = job_of(spec, photons)
     ctx = Context(device)
     if args.block or args.blocks_per_sm or args.aggregation:
         ctx.set_tuning(args.block, args.blocks_per_sm, args.aggregation)
-    nvox = sim.dim[0] * sim.dim[1] * sim.dim[2]
-    nout = nvox * sim.dim[3]
-    d_lab = torch.from_numpy(job.labels.ravel().copy()).to(f"cuda:{device}")
-    d_flu = torch.empty(nout, dtype=torch.float32, device=f"cuda:{device}")
-    d_det = torch.empty(sim.maxdetphotons * detp_columns(sim), dtype=torch.float32, device=f"cuda:{device}")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
-    stream = torch.cuda.current_stream()
     tuning = {"block_size": args.block, "blocks_per_sm": args.blocks_per_sm, "aggregation": args.aggregation,
               "source": "command line"}
     if not (args.block or args.blocks_per_sm or args.aggregation) and not args.no_autotune:
         # the project's autotuner: timed runs at half the photons over block sizes and aggregation modes.  A probe
-        # must be long against the launch's drain (the last, longest photons: ~7 ms here), or the drain's noise
+        # must be long against the launch's drain (the last, longest photons: ~5 ms here), or the drain's noise
         # decides the choice
-        tuning = dict(ctx.autotune(sim, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.5),
+        import numpy as np  # noqa: F401
+
+        from umcx_gb300 import detp_columns
+
+        s = job.sim
+        d_lab = torch.from_numpy(job.labels.ravel().copy()).to(f"cuda:{device}")
+        d_flu = torch.empty(s.dim[0] * s.dim[1] * s.dim[2] * s.dim[3], dtype=torch.float32, device=f"cuda:{device}")
+        d_det = torch.empty(max(1, s.maxdetphotons * detp_columns(s)), dtype=torch.float32, device=f"cuda:{device}")
+        tuning = dict(ctx.autotune(s, d_lab, job.media, job.detpos, d_flu, d_det, fraction=0.5),
                       source="autotune (50 % photon probes)")
+        del d_lab, d_flu, d_det
 
-    def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    for _ in range(args.warmup):
-        ctx.forward_device(sim, d_lab, job.media, job.detpos, d_flu, d_det, stream)
     sampler = ClockSampler(device)
     sampler.start()
-    kernel_ms, step_ms, results = [], [], []
-    barrier()
     t_all = time.perf_counter()
-    for _ in range(args.steps):
-        flush.fill_(1)
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        r = ctx.forward_device(sim, d_lab, job.media, job.detpos, d_flu, d_det, stream)
-        ev1.record(stream)
-        ev1.synchronize()
-        step_ms.append(ev0.elapsed_time(ev1))
-        kernel_ms.append(r.kernel_ms)
-        results.append(r)
-    barrier()
+    step_ms, kernel_ms, results = time_forward(ctx, job, photons, args.steps, args.warmup, device, flush, shard)
     wall_all = time.perf_counter() - t_all
     clocks = sampler.stop()
-
-    # end to end through the C ABI with host buffers: the caller's label volume in, the fluence and detected-photon
-    # rows out into output arrays it reuses from call to call (page-locked host memory, allocated and touched once
-    # outside the timed region)
-    def pinned(n, dtype):
-        return torch.ones(n, dtype=dtype, pin_memory=True).numpy()
-
-    h_lab = pinned(nvox, torch.uint8)
-    h_lab[:] = job.labels.reshape(-1)
-    h_med, h_det = job.media, job.detpos
-    h_flu = pinned(nout, torch.float32)
-    h_dp = pinned(max(1, sim.maxdetphotons * detp_columns(sim)), torch.float32)
-    e2e_ms = []
-    for _ in range(max(1, args.e2e_steps)):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        out = ctx.forward(sim, h_lab, h_med, h_det, fluence=h_flu, detp=h_dp)
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    r_host = out.result
-    h2d = nvox + 4 * 4 * sim.mediumnum + 4 * 4 * sim.detnum
-    d2h = nout * 4 + int(r_host.saved) * detp_columns(sim) * 4 + 96
+    e2e = time_e2e(ctx, job_of(spec, photons), photons, args.e2e_steps, flush)
 
     # max over ranks
     total_step_ms = sum(step_ms)
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_step_ms, statistics.mean(e2e_ms)], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_step_ms, e2e_mean = t.tolist()
-    else:
-        e2e_mean = statistics.mean(e2e_ms)
-
-    photons_all = int(args.photons) * ws
+    e2e_ms = e2e["ms_per_step"]
+    if shard is not None:
+        total_step_ms, e2e_ms = shard.max_over_ranks([total_step_ms, e2e_ms])
+    photons_all = photons * ws
     value = photons_all * args.steps / total_step_ms
-    e2e_value = photons_all / e2e_mean
+    e2e["value"] = photons_all / e2e_ms
+    e2e["ms_per_step"] = e2e_ms
     r0 = results[-1]
     kms = statistics.mean(kernel_ms)
-    fp32_ops = sum(getattr(r0, k) * v for k, v in OPS_FP32.items())
-    sfu_ops = sum(getattr(r0, k) * v for k, v in OPS_SFU.items())
     peaks = measure_peaks(device)
-    achieved_fp32 = fp32_ops / (kms * 1e-3) / 1e12
-    peak_fp32 = peaks["fp32_fma_per_s"] / 1e12
-    achieved_sfu = sfu_ops / (kms * 1e-3) / 1e12
-    peak_sfu = peaks["sfu_per_s"] / 1e12
-    atomics_per_s = r0.crossings / (kms * 1e-3)
-    issue_per_s = r0.steps * WARP_INST_PER_STEP / (kms * 1e-3)
-    issue_peak = peaks["sm_count"] * 4 * peaks["sm_clock_khz"] * 1e3
     peaks_file = ROOT / "MEASURED_PEAKS.json"
     hbm_peak = json.loads(peaks_file.read_text()).get("hbm_gbs") if peaks_file.exists() else 6800.0
-    traffic_alg = r0.crossings * 9.0  # label byte + fluence read-modify-write per crossing
     # the other forms first, while the GPU is still busy (the CPU baseline leaves it idle for seconds)
     forms = {}
     wanted = set() if args.no_forms else {f.strip() for f in args.forms.split(",") if f.strip()}
-    if rank == 0 and "adjoint" in wanted:
-        forms["adjoint"] = measure_adjoint(ctx, args)
-    if rank == 0 and "batched" in wanted:
-        forms["batched"] = measure_batched(ctx, args, device)
+    if rank == 0:
+        ctx.set_tuning(tuning["block_size"], tuning["blocks_per_sm"], tuning["aggregation"])
+        for name in ("c1", "cube60", "c3"):
+            if name in wanted:
+                forms[name] = measure_form(ctx, name, args, device, flush, peaks, hbm_peak)
+        if "adjoint" in wanted:
+            forms["adjoint"] = measure_adjoint(ctx, args)
+        if "batched" in wanted:
+            forms["batched"] = measure_batched(ctx, args, device)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_reference_run(args.cpu_photons, os.cpu_count() or 1)
 
     if rank == 0:
+        sim = job.sim
+        launches = 2 if (sim.issavevol and not (sim.flags & SIM_FP32_ACCUM)) else 1
         line = {
             "metric": METRIC, "value": value, "unit": "photons/ms", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_step_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (generated configuration)",
-            "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": int(args.photons), "grid": [60, 60, 60],
+            "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": photons, "grid": [60, 60, 60],
                        "gates": int(sim.dim[3]), "detectors": int(sim.detnum),
-                       "l2": "flushed between steps (256 MB write)", "parallelism": f"photon ranges x{ws}",
+                       "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"photon ranges x{ws}" + (" + GPU sum of volumes and tallies" if ws > 1 else ""),
                        "tuning": tuning},
-            "e2e": {"value": e2e_value, "unit": "photons/ms", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},
+            "e2e": e2e,
             # per step: the propagation kernel and the FP64 -> FP32 rounding of the output volume
-            "gpu_launches": args.steps * (2 if (sim.issavevol and not (sim.flags & SIM_FP32_ACCUM)) else 1),
+            "gpu_launches": args.steps * launches,
             "kernel_ms": kms,
-            "roofline": {"bound": "fp32", "achieved": achieved_fp32, "peak": peak_fp32,
-                         "unit": "Top/s (FP32 instructions, FMA = 1 op; peak measured live by an FMA loop)",
-                         "frac": achieved_fp32 / peak_fp32,
-                         "traffic": DRAM_BYTES_DEFAULT_LAUNCH if int(args.photons) == 10000000 else None,
-                         "ops_per_launch": fp32_ops,
-                         "events_per_launch": {k: int(getattr(r0, k)) for k in OPS_FP32},
-                         "sfu": {"achieved": achieved_sfu, "peak": peak_sfu, "frac": achieved_sfu / peak_sfu,
-                                 "unit": "Top/s"},
-                         "l2_atomics": {"achieved_per_s": atomics_per_s, "peak_per_s": peaks["l2_atomic_per_s"],
-                                        "frac": atomics_per_s / peaks["l2_atomic_per_s"]},
-                         "hbm": {"algorithmic_gbs": traffic_alg / (kms * 1e-3) / 1e9, "peak_gbs": hbm_peak},
-                         "issue": {"achieved_warp_inst_per_s": issue_per_s, "peak_warp_inst_per_s": issue_peak,
-                                   "frac": issue_per_s / issue_peak, "warp_inst_per_step": WARP_INST_PER_STEP,
-                                   "source": "instructions per step from the ncu capture of the default launch"}},
+            "roofline": roofline(r0, kms, peaks, hbm_peak, spec if photons == spec["photons"] else {}),
             "clocks": clocks,
             "physics": {"absorbed_percent": (r0.energy_total - r0.energy_escape) / r0.energy_total * 100,
                         "detected": int(r0.detected), "steps_per_photon": r0.steps / r0.launched,
@@ -454,10 +539,8 @@ def run_gpu_arm(args) -> None:
         if forms:
             line["forms"] = forms
         print(json.dumps(line), flush=True)
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    if shard is not None:
+        shard.close()
 
 
 def main():
@@ -473,12 +556,12 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--aggregation", type=int, default=0)
-    ap.add_argument("--no-forms", action="store_true", help="skip the adjoint and batched forms")
-    ap.add_argument("--forms", default="adjoint,batched", help="comma list of the extra forms to measure")
+    ap.add_argument("--no-forms", action="store_true", help="skip the other configurations and forms")
+    ap.add_argument("--forms", default="c1,cube60,c3,adjoint,batched", help="comma list of the extra forms to measure")
     ap.add_argument("--no-autotune", action="store_true", help="use the built-in launch defaults (forms: fixed)")
     ap.add_argument("--batch-sims", type=int, default=256)
-    ap.add_argument("--batch-scale", type=float, default=0.1,
-                    help="photon-budget scale of the batched form (1.0 = the full 5.4e8-photon batch, ~5 s/run)")
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="photon-budget scale of the batched form (1.0 = the full 5.4e8-photon batch, ~3.5 s/run)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":

@@ -59,3 +59,23 @@ def test_configs_parse_through_the_front_end():
         assert (s.dim[0], s.dim[3]) == (c["Domain"]["Dim"][0], 10)
         assert s.mediumnum == len(c["Domain"]["Media"]) and s.isreflect == 1
         assert set(np.unique(job.labels & 0x7F)) <= set(range(1, s.mediumnum))
+
+
+def test_benchmark_configurations_equal_the_pinned_ones():
+    """The benchmark's configurations 1-3 (umcx_gb300.workloads) are the ones the oracle is pinned on
+    (tests/golden/make_golden.py), apart from the photon count."""
+    import json
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import C1, C2, C3
+
+    from umcx_gb300.workloads import config1, config2, config3
+
+    for mine, pinned, n in ((config1(), C1, 1000000), (config2(), C2, 10000000), (config3(), C3, 100000000)):
+        a = json.loads(json.dumps(mine))
+        b = json.loads(json.dumps(pinned))
+        assert a["Session"].pop("Photons") == n
+        b["Session"].pop("Photons")
+        assert a == b
