@@ -12,6 +12,8 @@ size_t batch_smem(int nsim, int total_media, int block) {
 cudaError_t configure_batch_kernels() {
     cudaError_t e = allow_max_dynamic_smem(k_batch<false>);
     if (e == cudaSuccess) e = allow_max_dynamic_smem(k_batch<true>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_batch<false, true>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_batch<true, true>);
     return e;
 }
 
@@ -24,8 +26,14 @@ int batch_occupancy(bool reflect, int block, size_t smem) {
 
 void launch_batch(int grid, int block, size_t smem, bool reflect, const BParams& BP, const KBuffers& B,
                   cudaStream_t st) {
-    if (reflect) k_batch<true><<<grid, block, smem, st>>>(BP, B);
-    else k_batch<false><<<grid, block, smem, st>>>(BP, B);
+    if (BP.aggregate) {  // warp-aggregated deposits (the batch autotuner's alternative to plain atomics)
+        if (reflect) k_batch<true, true><<<grid, block, smem, st>>>(BP, B);
+        else k_batch<false, true><<<grid, block, smem, st>>>(BP, B);
+    } else if (reflect) {
+        k_batch<true><<<grid, block, smem, st>>>(BP, B);
+    } else {
+        k_batch<false><<<grid, block, smem, st>>>(BP, B);
+    }
 }
 
 }  // namespace umcx_dev

@@ -742,9 +742,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
             ev.left_mid = mid;
             ev.seg = p.lz;
             ev.w_before = p.lw;
-            // (int)fminf(maxgate - 1, floorf(x)) as one rounding conversion and an integer min (same value for
-            // every x: the conversion saturates like the reference's cast chain does on the device)
-            ev.gate = min(__float2int_rd((p.ly - P.tstart) * P.rtstep), P.maxgate - 1);
+            ev.gate = deposit_gate(P, p);
             ev.dep_val = deposit_value<STRICT>(P, p, m);
             if (RESET_SEGMENT || P.issavevol) {
                 p.lw = p.pw;
@@ -929,14 +927,20 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
     return false;
 }
 
-// One iteration of the forward kernel for an active photon with plain fluence atomics: advance() with the
-// partial-path update (L286-288) and the deposit (L289-291, L359-363) made where the voxel crossing is handled, so
-// that neither the deposit's address and value nor the crossing's bookkeeping stay live through the scattering code.
-// Returns true when the photon ended.  (The warp-aggregated mode deposits after the divergent part instead: its
-// __match_any_sync needs the whole warp.)
-template <bool STRICT, bool REFLECT, bool SAVEDET, int REP, class LV>
-__device__ __forceinline__ bool forward_step(const KParams& P, const KBuffers& B, const LV& labels, const Medium* sm,
-                                             Photon& p, Counters& c, float* ppath_lane, const Replica& rep) {
+// One iteration for an active photon: a voxel step and, at a voxel change, the bookkeeping, time-gate test, boundary
+// handling and label update of MCX_photon::sprint (L281-314); then a scatter when the free path is used up
+// (L272-274).  What a kernel records is done in place by two callbacks -- at a crossing, on_cross(mid, m) with the
+// photon still holding the segment just ended (p.lz: path since the last deposit, p.lw: weight there, p.pw: weight
+// now, p.lastvox: the voxel left, of medium mid), and after a scatter in medium mid, on_scatter(mid) -- so that
+// nothing a crossing records stays live through the scattering code.  Returns true when the photon ended.
+// RESET_SEGMENT resets the deposit segment at every crossing even when no volume is saved (per-voxel path lengths
+// for the adjoint and the replay); trajectories do not depend on it.  Every kernel advances photons with this
+// function (the warp-aggregated forward and batched instances with advance(), which performs the same operations
+// in the same order), so a replayed photon follows the forward pass's trajectory.
+// PV is KParams (a single simulation) or SimDesc (a simulation of a batch).
+template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV, class LV, class OnCross, class OnScatter>
+__device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const Medium* sm, Photon& p, Counters& c,
+                                            OnCross&& on_cross, OnScatter&& on_scatter) {
     bool term = false;
     if (p.lx > 0.f) {
         const unsigned mid = p.media & UMCX_LABEL_MASK;
@@ -953,23 +957,17 @@ __device__ __forceinline__ bool forward_step(const KParams& P, const KBuffers& B
         term = capped;
         if (!capped && newvox != p.lastvox) {
             c.cross++;
-            // the next voxel's label first: its load overlaps the deposit below
+            // the next voxel's label first: its load overlaps the recording below
             const bool late = p.ly > P.tend;
             unsigned newmedia = (newvox >= 0 && !late) ? labels(newvox) : 0u;
-            if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && mid > 0 &&
-                index_ok(&B.stats->error, mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
-                ppath_lane[(mid - 1) * blockDim.x] += p.lz;
-            if (P.issavevol) {
-                const int gate = min(__float2int_rd((p.ly - P.tstart) * P.rtstep), P.maxgate - 1);
-                if (gate >= 0)
-                    deposit_add<REP>(B, p.lastvox + gate * static_cast<int>(P.dimxyz), deposit_value<STRICT>(P, p, m),
-                                     rep);
+            on_cross(mid, m);
+            if (RESET_SEGMENT || P.issavevol) {
                 p.lw = p.pw;
                 p.lz = 0.f;
             }
             const float n2 = sm[newmedia & UMCX_LABEL_MASK].a.w;
             term = late || newvox < 0 || ((newmedia & UMCX_LABEL_MASK) == 0 && mid != 0);
-            if (REFLECT && !late && m.a.w != n2) {
+            if (REFLECT && reflect_on(P) && !late && m.a.w != n2) {
                 rare_count(kRareRefl);
                 if (reflect<STRICT>(p, m.a.w, n2)) {
                     term = newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0;
@@ -986,10 +984,35 @@ __device__ __forceinline__ bool forward_step(const KParams& P, const KBuffers& B
         }
     }
     if (!term && p.lx <= 0.f) {
-        scatter<STRICT>(p, sm[p.media & UMCX_LABEL_MASK]);
+        const unsigned mid = p.media & UMCX_LABEL_MASK;
+        scatter<STRICT>(p, sm[mid]);
         c.scat++;
+        on_scatter(mid);
     }
     return term;
+}
+
+// the time gate of a deposit at the photon's current time: (int)fminf(maxgate - 1, floorf(x)) as one rounding
+// conversion and an integer min (same value for every x: the conversion saturates like the reference's cast chain
+// does on the device); negative before tstart
+template <class PV>
+__device__ __forceinline__ int deposit_gate(const PV& P, const Photon& p) {
+    return min(__float2int_rd((p.ly - P.tstart) * P.rtstep), P.maxgate - 1);
+}
+
+// the forward kernels' crossing record: partial path of the medium left (L286-288) and the fluence deposit
+// (L289-291, L359-363) through deposit(voxel, gate, value)
+template <bool STRICT, bool SAVEDET, class PV, class Deposit>
+__device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, unsigned mid, const Medium& m,
+                                                float* ppath_lane, int* err, Deposit&& deposit) {
+    if constexpr (SAVEDET) {
+        if ((P.savedetflag & UMCX_DET_PPATH) && mid > 0 && index_ok(err, mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
+            ppath_lane[(mid - 1) * blockDim.x] += p.lz;
+    }
+    if (P.issavevol) {
+        const int gate = deposit_gate(P, p);
+        if (gate >= 0) deposit(p.lastvox, gate, deposit_value<STRICT>(P, p, m));
+    }
 }
 
 // =============================================================================================== forward kernel
@@ -1063,11 +1086,20 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
             deposit_converged<REP>(B, true, aggbuf, tid, lane, dep_idx, dep_val, replica);
             term = ev.term;
         } else if (active) {
-            term = forward_step<STRICT, REFLECT, SAVEDET, REP>(P, B, labels, sm, p, c, ppath + tid, replica);
+            term = photon_step<STRICT, REFLECT, false>(
+                P, labels, sm, p, c,
+                [&](unsigned mid, const Medium& m) {
+                    record_crossing<STRICT, SAVEDET>(P, p, mid, m, ppath + tid, &B.stats->error,
+                                                     [&](int vox, int gate, float v) {
+                                                         deposit_add<REP>(B, vox + gate * static_cast<int>(P.dimxyz), v,
+                                                                          replica);
+                                                     });
+                },
+                [](unsigned) {});
         }
         if (term) {
             count_stopped(p);
-            if (!AGG) c.steps += p.nsteps;  // forward_step does not count steps one by one
+            if (!AGG) c.steps += p.nsteps;  // photon_step does not count steps one by one
             if (SAVEDET) {
                 const bool tdet = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
                 append_detected(P, B, lane, tdet, p, [&](int d, unsigned long long slot) {
@@ -1170,54 +1202,54 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
             if (out_of_budget(B, iter, lane)) break;
         }
 
-        int dep_idx = -1;
-        float dep_val = 0.f;
-        Event ev;
-        ev.term = false;
+        bool term = false;
         if (active) {
-            advance<false, REFLECT, true>(P, labels(), sm, p, ev, c);
-            if (ev.crossed) {
-                const unsigned m = ev.left_mid;
-                if ((P.savedetflag & UMCX_DET_PPATH) && m > 0 &&
-                    index_ok(&B.stats->error, m - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
-                    ppath[(m - 1) * bd + tid] += ev.seg;
-                float F = 0.f, dF = 0.f;
-                if (P.issavevol && ev.gate >= 0) {
-                    dep_idx = ev.left_vox + ev.gate * static_cast<int>(P.dimxyz);
-                    dep_val = ev.dep_val;
-                    F = ev.dep_val;
-                    // derivative of this deposit with respect to its own label's mua along the fixed path
-                    if (P.outputtype == UMCX_OUT_ENERGY) {
-                        dF = ev.seg * p.pw;  // d(w0 (1 - e^-mua l))/dmua = l w1
-                    } else {
-                        // fluence = integral of w over the segment; derivative -w0 (1 - (1 + x) e^-x) / mua^2,
-                        // x = mua l, by its series for small x (also the mua -> 0 limit -w0 l^2 / 2)
-                        const float mua = sm[m].a.x;
-                        const float x = mua * ev.seg;
-                        float i1;
-                        if (x < 0.1f) {
-                            i1 = ev.seg * ev.seg *
-                                 (0.5f + x * (-1.f / 3.f + x * (0.125f + x * (-1.f / 30.f + x * (1.f / 144.f)))));
-                        } else {
-                            i1 = (1.f - (1.f + x) * expf(-x)) / (mua * mua);
+            term = photon_step<false, REFLECT, true>(
+                P, labels(), sm, p, c,
+                [&](unsigned m, const Medium& med) {
+                    const float seg = p.lz;  // path in the voxel left (the segment is reset at every crossing)
+                    if ((P.savedetflag & UMCX_DET_PPATH) && m > 0 &&
+                        index_ok(&B.stats->error, m - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
+                        ppath[(m - 1) * bd + tid] += seg;
+                    float F = 0.f, dF = 0.f;
+                    if (P.issavevol) {
+                        const int gate = deposit_gate(P, p);
+                        if (gate >= 0) {
+                            F = deposit_value<false>(P, p, med);
+                            deposit_add(B, p.lastvox + gate * static_cast<int>(P.dimxyz), F);
+                            // derivative of this deposit with respect to its own label's mua along the fixed path
+                            if (P.outputtype == UMCX_OUT_ENERGY) {
+                                dF = seg * p.pw;  // d(w0 (1 - e^-mua l))/dmua = l w1
+                            } else {
+                                // fluence = integral of w over the segment; derivative -w0 (1 - (1 + x) e^-x) / mua^2,
+                                // x = mua l, by its series for small x (also the mua -> 0 limit -w0 l^2 / 2)
+                                const float mua = med.a.x;
+                                const float x = mua * seg;
+                                float i1;
+                                if (x < 0.1f) {
+                                    i1 = seg * seg *
+                                         (0.5f + x * (-1.f / 3.f + x * (0.125f + x * (-1.f / 30.f + x * (1.f / 144.f)))));
+                                } else {
+                                    i1 = (1.f - (1.f + x) * expf(-x)) / (mua * mua);
+                                }
+                                dF = -p.lw * i1;
+                            }
                         }
-                        dF = -ev.w_before * i1;
                     }
-                }
-                S += F;
-                Lk[m * bd + tid] += ev.seg;
-                Qk[m * bd + tid] += ev.seg * S;
-                Tk[m * bd + tid] += F * ev.seg;
-                Ek[m * bd + tid] += dF;
-            }
-            if (ev.scattered) {
-                Ck[ev.scat_mid * bd + tid] += 1.f;
-                Rk[ev.scat_mid * bd + tid] += S;
-            }
+                    S += F;
+                    Lk[m * bd + tid] += seg;
+                    Qk[m * bd + tid] += seg * S;
+                    Tk[m * bd + tid] += F * seg;
+                    Ek[m * bd + tid] += dF;
+                },
+                [&](unsigned m) {
+                    Ck[m * bd + tid] += 1.f;
+                    Rk[m * bd + tid] += S;
+                });
         }
-        deposit_converged(B, false, nullptr, tid, lane, dep_idx, dep_val);
-        if (ev.term) {
+        if (term) {
             count_stopped(p);
+            c.steps += p.nsteps;  // photon_step does not count steps one by one
             // detection (L429-435): the terminating lane appends its records, one atomic per detector hit, with
             // the extended record (photon index, exit weight and time, per-label path and scatter counts)
             const bool tdet = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend;
@@ -1308,14 +1340,17 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
             if (out_of_budget(B, iter, lane)) break;
         }
         if (active) {
-            Event ev;
-            advance<false, REFLECT, true>(P, global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)), sm,
-                                          p, ev, c);
-            const unsigned long long jidx = static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + ev.left_vox;
-            if (ev.crossed && ev.left_vox >= 0 && index_ok(&B.stats->error, jidx, UMCX_EXTENT(B, n_jacobian), kSiteJacobian))
-                atomicAdd(B.jacobian + jidx, -rec.weight * ev.seg);
-            if (ev.term) {
+            const bool term = photon_step<false, REFLECT, true>(
+                P, global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)), sm, p, c,
+                [&](unsigned, const Medium&) {
+                    const unsigned long long jidx = static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + p.lastvox;
+                    if (index_ok(&B.stats->error, jidx, UMCX_EXTENT(B, n_jacobian), kSiteJacobian))
+                        atomicAdd(B.jacobian + jidx, -rec.weight * p.lz);
+                },
+                [](unsigned) {});
+            if (term) {
                 count_stopped(p);
+                c.steps += p.nsteps;
                 const bool same = (p.media & UMCX_LABEL_DET) && p.ly <= P.tend && det_hit(P.det[rec.det - 1], p) &&
                                   p.pw == rec.weight;
                 if (!same) mismatch++;
@@ -1369,7 +1404,7 @@ __device__ __forceinline__ void deposit_add64(const KBuffers& B, long long idx, 
 // their outputs stay in L2, while the tail of one simulation overlaps the start of the next.
 // Shared memory: SimDesc[nsim] | u64 begin[nsim + 1] (padded to 16 B) | Medium[total_media] | float aggbuf[blockDim] |
 // double escape, total[blockDim]
-template <bool REFLECT>
+template <bool REFLECT, bool AGG = false>
 __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers B) {
     extern __shared__ float4 smem4[];
     SimDesc* sd = reinterpret_cast<SimDesc*>(smem4);
@@ -1438,21 +1473,22 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
             if (out_of_budget(B, iter, lane)) break;
         }
 
-        long long dep_idx = -1;
-        float dep_val = 0.f;
-        Event ev;
-        ev.term = false;
-        if (active) {
-            const SimDesc& S = sd[sim];
-            const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
-            advance<false, REFLECT, false>(S, lab, sm + S.media_base, p, ev, c);
-            const bool dep = ev.crossed && S.issavevol && ev.gate >= 0;
-            dep_idx = dep ? static_cast<long long>(S.out_off) + ev.left_vox +
-                                static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz)
-                          : -1;
-            dep_val = dep ? ev.dep_val : 0.f;
-        }
-        if (BP.aggregate) {
+        bool term = false;
+        if (AGG) {  // deposits after the divergent part, aggregated per warp
+            long long dep_idx = -1;
+            float dep_val = 0.f;
+            Event ev;
+            ev.term = false;
+            if (active) {
+                const SimDesc& S = sd[sim];
+                const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
+                advance<false, REFLECT, false>(S, lab, sm + S.media_base, p, ev, c);
+                const bool dep = ev.crossed && S.issavevol && ev.gate >= 0;
+                dep_idx = dep ? static_cast<long long>(S.out_off) + ev.left_vox +
+                                    static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz)
+                              : -1;
+                dep_val = dep ? ev.dep_val : 0.f;
+            }
             const unsigned hm = __ballot_sync(kFull, dep_idx >= 0);
             if (__popc(hm) > 1) {
                 const unsigned grp = __match_any_sync(kFull, dep_idx >= 0 ? static_cast<unsigned long long>(dep_idx) : ~0ULL);
@@ -1468,11 +1504,23 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
             } else if (dep_idx >= 0) {
                 deposit_add64(B, dep_idx, dep_val);
             }
-        } else if (dep_idx >= 0) {
-            deposit_add64(B, dep_idx, dep_val);
+            term = ev.term;
+        } else if (active) {  // plain atomics where the crossing is handled
+            const SimDesc& S = sd[sim];
+            const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
+            term = photon_step<false, REFLECT, false>(
+                S, lab, sm + S.media_base, p, c,
+                [&](unsigned mid, const Medium& m) {
+                    record_crossing<false, false>(S, p, mid, m, nullptr, &B.stats->error, [&](int vox, int gate, float v) {
+                        deposit_add64(B, static_cast<long long>(S.out_off) + vox + static_cast<long long>(gate) * S.dimxyz,
+                                      v);
+                    });
+                },
+                [](unsigned) {});
         }
-        if (ev.term) {
+        if (term) {
             count_stopped(p);
+            if (!AGG) c.steps += p.nsteps;  // photon_step does not count steps one by one
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
                 etally[blockDim.x + tid] += p.launchw;
                 etally[tid] += p.pw;
