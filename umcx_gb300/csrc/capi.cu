@@ -796,7 +796,7 @@ SimDesc make_desc(const umcx_sim* s, unsigned media_base, unsigned long long lab
     d.issavevol = P.issavevol;
     d.outputtype = P.outputtype;
     d.srctype = P.srctype;
-    d.step_cap = P.step_cap;
+    d.pad = 0;
     d.media_base = media_base;
     d.tstart = P.tstart;
     d.tend = P.tend;

@@ -71,7 +71,6 @@ inline KParams make_params(const umcx_sim* s, const float* detpos) {
     P.maxdetphotons = s->issavedet ? s->maxdetphotons : 0u;
     P.cols = umcx_detp_columns(s);
     P.ppathlen = (s->issavedet && (s->savedetflag & UMCX_DET_PPATH)) ? s->mediumnum : 0;
-    P.step_cap = kDefaultStepCap;
     for (int k = 0; k < 4; k++) P.seeds[k] = s->seeds[k];
     P.srcpos = make_float4(s->srcpos[0], s->srcpos[1], s->srcpos[2], 1.f);
     P.srcdir = make_float4(s->srcdir[0], s->srcdir[1], s->srcdir[2], 0.f);
