@@ -433,54 +433,6 @@ __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, boo
     return c ? vox_index(P, p.ix, p.iy, p.iz) : p.lastvox;
 }
 
-// step() for photon_step: the same arithmetic, but the photon keeps no voxel index across iterations -- on a
-// crossing *oldvox receives the index of the voxel left (from the coordinates before the update) and the return value
-// is the index of the voxel entered (-1 outside the grid); without a crossing it returns -1.
-template <bool STRICT, class PV>
-__device__ __forceinline__ int step_indexed(const PV& P, Photon& p, const Medium& m, bool* crossed, float* moved,
-                                            int* oldvox) {
-    const int bx = p.vx > 0.f, by = p.vy > 0.f, bz = p.vz > 0.f;
-    const float2 hxy = __fmul2_rn(__fadd2_rn(make_float2(static_cast<float>(p.ix + bx), static_cast<float>(p.iy + by)),
-                                             make_float2(-p.px, -p.py)),
-                                  make_float2(p.rx, p.ry));
-    const float hx = fabsf(hxy.x), hy = fabsf(hxy.y);
-    const float hz = fabsf((static_cast<float>(p.iz + bz) - p.pz) * p.rz);
-    float dist = fminf(fminf(hx, hy), hz);
-    p.flip = (dist == hx ? 0 : (dist == hy ? 1 : 2));
-    const float mus = m.a.y;
-    const float used = fminf(dist * mus, p.lx);
-    *crossed = (used != p.lx);
-    if constexpr (STRICT) {
-        dist = (mus == 0.f) ? dist : (used / mus);
-        const float2 pxy = __fadd2_rn(make_float2(p.px, p.py), __fmul2_rn(make_float2(dist, dist), make_float2(p.vx, p.vy)));
-        p.px = pxy.x;
-        p.py = pxy.y;
-        p.pz = p.pz + dist * p.vz;
-        p.pw = p.pw * expf(-m.a.x * dist);
-        p.lx -= used;
-        p.ly += dist * m.a.w * kOneOverC0;
-    } else {
-        dist = (mus == 0.f) ? dist : (used * m.b.x);
-        const float2 pxy = __ffma2_rn(make_float2(dist, dist), make_float2(p.vx, p.vy), make_float2(p.px, p.py));
-        p.px = pxy.x;
-        p.py = pxy.y;
-        p.pz = p.pz + dist * p.vz;
-        p.pw = p.pw * __expf(-m.a.x * dist);
-        p.lx -= used;
-        p.ly += dist * m.b.w;
-    }
-    p.lz += dist;
-    *moved = dist;
-    if (!*crossed) return -1;
-    *oldvox = static_cast<int>(static_cast<unsigned>(p.ix) * P.dimyz + static_cast<unsigned>(p.iy) * static_cast<unsigned>(P.nz) +
-                               static_cast<unsigned>(p.iz));
-    const int f = p.flip;
-    p.ix += (f == 0) * (2 * bx - 1);
-    p.iy += (f == 1) * (2 * by - 1);
-    p.iz += (f == 2) * (2 * bz - 1);
-    return vox_index(P, p.ix, p.iy, p.iz);
-}
-
 // MCX_photon::scatter, L364-380
 template <bool STRICT>
 __device__ __forceinline__ void scatter(Photon& p, const Medium& m) {
@@ -976,12 +928,10 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
 
 // One iteration for an active photon: a voxel step and, at a voxel change, the bookkeeping, time-gate test, boundary
 // handling and label update of MCX_photon::sprint (L281-314); then a scatter when the free path is used up
-// (L272-274).  What a kernel records is done in place by two callbacks -- at a crossing, on_cross(mid, m, vox) with
-// the photon still holding the segment just ended (p.lz: path since the last deposit, p.lw: weight there, p.pw:
-// weight now) and vox the index of the voxel left, of medium mid; after a scatter in medium mid, on_scatter(mid) --
-// so that nothing a crossing records stays live through the scattering code.  The photon's voxel index is not kept
-// between iterations (step_indexed recomputes it from the coordinates at a crossing), which leaves the loop a
-// register.  Returns true when the photon ended.
+// (L272-274).  What a kernel records is done in place by two callbacks -- at a crossing, on_cross(mid, m) with the
+// photon still holding the segment just ended (p.lz: path since the last deposit, p.lw: weight there, p.pw: weight
+// now, p.lastvox: the voxel left, of medium mid), and after a scatter in medium mid, on_scatter(mid) -- so that
+// nothing a crossing records stays live through the scattering code.  Returns true when the photon ended.
 // RESET_SEGMENT resets the deposit segment at every crossing even when no volume is saved (per-voxel path lengths
 // for the adjoint and the replay); trajectories do not depend on it.  Every kernel advances photons with this
 // function (the warp-aggregated forward and batched instances with advance(), which performs the same operations
@@ -996,8 +946,7 @@ __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const
         const Medium m = sm[mid];
         bool crossed;
         float moved;
-        int oldvox;
-        const int newvox = step_indexed<STRICT>(P, p, m, &crossed, &moved, &oldvox);
+        int newvox = step<STRICT>(P, p, m, &crossed, &moved);
         // (the lane's step count is taken from p.nsteps when the photon ends)
         // zero-progress guard and step cap, as in advance()
         if (moved == 0.f) p.media += 0x10000u;
@@ -1005,12 +954,12 @@ __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const
         const bool capped = ++p.nsteps > kDefaultStepCap || p.media >= (kZeroStepLimit << 16);
         p.media |= capped ? kStoppedBit : 0u;
         term = capped;
-        if (!capped && crossed) {
+        if (!capped && newvox != p.lastvox) {
             c.cross++;
             // the next voxel's label first: its load overlaps the recording below
             const bool late = p.ly > P.tend;
             unsigned newmedia = (newvox >= 0 && !late) ? labels(newvox) : 0u;
-            on_cross(mid, m, oldvox);
+            on_cross(mid, m);
             if (RESET_SEGMENT || P.issavevol) {
                 p.lw = p.pw;
                 p.lz = 0.f;
@@ -1022,11 +971,15 @@ __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const
                 if (reflect<STRICT>(p, m.a.w, n2)) {
                     term = newvox < 0 || (newmedia & UMCX_LABEL_MASK) == 0;
                 } else {
-                    term = false;  // put back into the voxel it was leaving (coordinates restored by reflect)
+                    term = false;
+                    newvox = p.lastvox;
                     newmedia = p.media;
                 }
             }
-            if (!term) p.media = newmedia;
+            if (!term) {
+                p.lastvox = newvox;
+                p.media = newmedia;
+            }
         }
     }
     if (!term && p.lx <= 0.f) {
@@ -1049,7 +1002,7 @@ __device__ __forceinline__ int deposit_gate(const PV& P, const Photon& p) {
 // the forward kernels' crossing record: partial path of the medium left (L286-288) and the fluence deposit
 // (L289-291, L359-363) through deposit(voxel, gate, value)
 template <bool STRICT, bool SAVEDET, class PV, class Deposit>
-__device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, unsigned mid, const Medium& m, int vox,
+__device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, unsigned mid, const Medium& m,
                                                 float* ppath_lane, int* err, Deposit&& deposit) {
     if constexpr (SAVEDET) {
         if ((P.savedetflag & UMCX_DET_PPATH) && mid > 0 && index_ok(err, mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
@@ -1057,7 +1010,7 @@ __device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, un
     }
     if (P.issavevol) {
         const int gate = deposit_gate(P, p);
-        if (gate >= 0) deposit(vox, gate, deposit_value<STRICT>(P, p, m));
+        if (gate >= 0) deposit(p.lastvox, gate, deposit_value<STRICT>(P, p, m));
     }
 }
 
@@ -1134,8 +1087,8 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
         } else if (active) {
             term = photon_step<STRICT, REFLECT, false>(
                 P, labels, sm, p, c,
-                [&](unsigned mid, const Medium& m, int vox) {
-                    record_crossing<STRICT, SAVEDET>(P, p, mid, m, vox, ppath + tid, &B.stats->error,
+                [&](unsigned mid, const Medium& m) {
+                    record_crossing<STRICT, SAVEDET>(P, p, mid, m, ppath + tid, &B.stats->error,
                                                      [&](int vox, int gate, float v) {
                                                          deposit_add<REP>(B, vox + gate * static_cast<int>(P.dimxyz), v,
                                                                           replica);
@@ -1252,7 +1205,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
         if (active) {
             term = photon_step<false, REFLECT, true>(
                 P, labels(), sm, p, c,
-                [&](unsigned m, const Medium& med, int vox) {
+                [&](unsigned m, const Medium& med) {
                     const float seg = p.lz;  // path in the voxel left (the segment is reset at every crossing)
                     if ((P.savedetflag & UMCX_DET_PPATH) && m > 0 &&
                         index_ok(&B.stats->error, m - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
@@ -1262,7 +1215,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                         const int gate = deposit_gate(P, p);
                         if (gate >= 0) {
                             F = deposit_value<false>(P, p, med);
-                            deposit_add(B, vox + gate * static_cast<int>(P.dimxyz), F);
+                            deposit_add(B, p.lastvox + gate * static_cast<int>(P.dimxyz), F);
                             // derivative of this deposit with respect to its own label's mua along the fixed path
                             if (P.outputtype == UMCX_OUT_ENERGY) {
                                 dF = seg * p.pw;  // d(w0 (1 - e^-mua l))/dmua = l w1
@@ -1388,8 +1341,8 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
         if (active) {
             const bool term = photon_step<false, REFLECT, true>(
                 P, global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)), sm, p, c,
-                [&](unsigned, const Medium&, int vox) {
-                    const unsigned long long jidx = static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + vox;
+                [&](unsigned, const Medium&) {
+                    const unsigned long long jidx = static_cast<unsigned long long>(rec.det - 1) * P.dimxyz + p.lastvox;
                     if (index_ok(&B.stats->error, jidx, UMCX_EXTENT(B, n_jacobian), kSiteJacobian))
                         atomicAdd(B.jacobian + jidx, -rec.weight * p.lz);
                 },
@@ -1556,8 +1509,8 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
             const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
             term = photon_step<false, REFLECT, false>(
                 S, lab, sm + S.media_base, p, c,
-                [&](unsigned mid, const Medium& m, int left) {
-                    record_crossing<false, false>(S, p, mid, m, left, nullptr, &B.stats->error, [&](int vox, int gate, float v) {
+                [&](unsigned mid, const Medium& m) {
+                    record_crossing<false, false>(S, p, mid, m, nullptr, &B.stats->error, [&](int vox, int gate, float v) {
                         deposit_add64(B, static_cast<long long>(S.out_off) + vox + static_cast<long long>(gate) * S.dimxyz,
                                       v);
                     });
