@@ -54,17 +54,21 @@ METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates
 # that photon count.  None where no capture exists; the line then reports null for those fractions.
 FORWARD = {
     "c2": {"json": CONFIG, "photons": 10000000, "workload": WORKLOAD,
-           "warp_inst_per_step": None, "dram_bytes": None},
+           # profiles/k_forward_workloads.md: 3.9196e10 warp instructions / 3.4361e9 steps; 93.3 MB + 3.066 GB
+           "warp_inst_per_step": 11.41, "dram_bytes": 93263104 + 3066302464},
     "c1": {"json": config1(), "photons": 1000000, "steps": 20,
            "workload": "homogeneous 60^3 cube, pencil beam, one 5 ns gate, no reflection (configuration 1)",
-           "warp_inst_per_step": None, "dram_bytes": None},
+           # 4.1648e9 / 1.9618e8 steps (at 1e6 photons the launch's drain is a large share); 13.9 MB read
+           "warp_inst_per_step": 21.23, "dram_bytes": 13947136},
     "cube60": {"args": ["--bench", "cube60"], "photons": 100000000, "steps": 5,
                "workload": "the reference's cube60 benchmark: configuration 1 plus four saved detectors, 1e8 photons "
                            "(published: 175 075 photons/ms on an RTX 5090)",
-               "warp_inst_per_step": None, "dram_bytes": None},
+               # 1.8144e11 / 1.9626e10 steps; 14.4 MB read (the 1.7 MB FP64 volume stays in L2)
+               "warp_inst_per_step": 9.245, "dram_bytes": 14393344 + 1792},
     "c3": {"json": config3(), "photons": 100000000, "steps": 5,
            "workload": "200^3 layered domain of 0.005 mm voxels with a cylinder, disk source, 1 ns gate (configuration 3)",
-           "warp_inst_per_step": None, "dram_bytes": None},
+           # 2.8430e11 / 2.9111e10 steps; 69.4 MB read + 10.9 GB of FP64 accumulator lines written back
+           "warp_inst_per_step": 9.766, "dram_bytes": 69396736 + 10901503744},
 }
 
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
@@ -446,8 +450,8 @@ def run_gpu_arm(args) -> None:
     device = local if ws > 1 else 0
     torch.cuda.set_device(device)
 
-    spec = FORWARD["c2"]
-    photons = int(args.photons)
+    spec = FORWARD[args.workload]
+    photons = int(args.photons) if args.photons else int(spec["photons"])
     job = job_of(spec, photons)
     ctx = Context(device)
     if args.block or args.blocks_per_sm or args.aggregation:
@@ -513,10 +517,11 @@ def run_gpu_arm(args) -> None:
         sim = job.sim
         launches = 2 if (sim.issavevol and not (sim.flags & SIM_FP32_ACCUM)) else 1
         line = {
-            "metric": METRIC, "value": value, "unit": "photons/ms", "n_gpus": ws, "steps": args.steps,
+            "metric": METRIC if args.workload == "c2" else f"photons/ms ({spec['workload']})", "value": value,
+            "unit": "photons/ms", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_step_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (generated configuration)",
-            "config": {"workload": WORKLOAD, "photons_per_step_per_gpu": photons, "grid": [60, 60, 60],
+            "config": {"workload": spec["workload"], "photons_per_step_per_gpu": photons, "grid": list(sim.dim[:3]),
                        "gates": int(sim.dim[3]), "detectors": int(sim.detnum),
                        "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"photon ranges x{ws}" + (" + GPU sum of volumes and tallies" if ws > 1 else ""),
@@ -549,7 +554,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--photons", type=float, default=1e7)
+    ap.add_argument("--photons", type=float, default=0, help="photons per step (default: the workload's own)")
+    ap.add_argument("--workload", default="c2", choices=sorted(FORWARD),
+                    help="the timed configuration (default: configuration 2, the headline; the others for profiling)")
     ap.add_argument("--cpu-photons", type=int, default=1000000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
