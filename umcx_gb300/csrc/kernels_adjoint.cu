@@ -6,8 +6,8 @@ namespace umcx_dev {
 
 size_t adjoint_smem(const KParams& P, int block) {
     const size_t K = static_cast<size_t>(P.mediumnum);
-    return 2 * K * block * sizeof(double) + K * sizeof(Medium) + static_cast<size_t>(P.ppathlen) * block * sizeof(float) +
-           6 * K * block * sizeof(float) + 3 * block * sizeof(double);  // + energy tallies and photon indices
+    return (2 * K + 2) * sizeof(double) + K * sizeof(Medium) + static_cast<size_t>(P.ppathlen) * block * sizeof(float) +
+           6 * K * block * sizeof(float) + block * sizeof(unsigned long long);  // + photon indices
 }
 
 cudaError_t configure_adjoint_kernels() {

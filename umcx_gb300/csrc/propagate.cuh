@@ -1129,16 +1129,19 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
 //               = (cnt_k S - R_k)/mus_k - (L_k S - Q_k + T_k)   with R_k += S at each scatter, T_k += F_j l_j
 // so each deposit and each scatter updates one label's tallies (O(1) per event).
 //
-// Shared memory: double ga[K][bd], gs[K][bd] | Medium[K] | float ppath[ppathlen][bd] | float L, cnt, Q, T, E, R[K][bd] |
-// double total, escape[bd] | u64 photon index[bd]
+// Shared memory: double ga[K], gs[K], total, escape | Medium[K] | float ppath[ppathlen][bd] |
+// float L, cnt, Q, T, E, R[K][bd] | u64 photon index[bd]
 template <bool REFLECT>
 __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffers B) {
     extern __shared__ double smem8[];
     const unsigned bd = blockDim.x;
     const int K = P.mediumnum;
-    double* ga = smem8;
-    double* gs = ga + K * bd;
-    Medium* sm = reinterpret_cast<Medium*>(gs + K * bd);
+    // the CTA's FP64 accumulators of the per-label gradients and of the energy tallies, added to with shared-memory
+    // atomics once per photon (per-lane copies would take shared memory from the L1 that caches the labels)
+    double* ga = smem8;   // [K]
+    double* gs = ga + K;  // [K]
+    double* et = gs + K;  // [2]: total, escape
+    Medium* sm = reinterpret_cast<Medium*>(et + 2);
     float* ppath = reinterpret_cast<float*>(sm + K);
     float* Lk = ppath + P.ppathlen * bd;
     float* Ck = Lk + K * bd;
@@ -1146,19 +1149,15 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     float* Tk = Qk + K * bd;
     float* Ek = Tk + K * bd;
     float* Rk = Ek + K * bd;
-    // touched once per photon, so kept out of the loop's registers: FP64 energy tallies and the photon index
-    double* etally = reinterpret_cast<double*>(Rk + K * bd);                    // [2][bd]: total, escape
-    unsigned long long* cur = reinterpret_cast<unsigned long long*>(etally + 2 * bd);  // [bd]
+    // touched once per photon, so kept out of the loop's registers: the photon index
+    unsigned long long* cur = reinterpret_cast<unsigned long long*>(Rk + K * bd);  // [bd]
     // the label view is built from kernel parameters where it is used, so it holds no registers in the loop
     auto labels = [&]() { return global_labels(B, 0, P.dimxyz, static_cast<unsigned>(P.mediumnum)); };
+    for (int k = threadIdx.x; k < 2 * K + 2; k += bd) ga[k] = 0.0;
     load_media(P, B.media, sm);
 
     const unsigned tid = threadIdx.x;
     const unsigned lane = lane_id();
-    for (int k = 0; k < K; k++) {
-        ga[k * bd + tid] = 0.0;
-        gs[k * bd + tid] = 0.0;
-    }
     PhotonFeed feed;
     feed.init(B.counter, static_cast<unsigned long long>(blockIdx.x) * bd + tid, P.nphoton,
               static_cast<unsigned long long>(gridDim.x) * bd);
@@ -1166,8 +1165,6 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     p.media = 0;
     p.lastvox = -1;
     bool active = false, done = false;
-    etally[tid] = 0.0;
-    etally[bd + tid] = 0.0;
     cur[tid] = 0;
     Counters c;
     float S = 0.f;
@@ -1268,32 +1265,28 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                 }
             });
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
-                etally[tid] += static_cast<double>(p.launchw);
-                etally[bd + tid] += static_cast<double>(p.pw);
+                atomicAdd(et, static_cast<double>(p.launchw));
+                atomicAdd(et + 1, static_cast<double>(p.pw));
             }
             for (int q = 0; q < K; q++) {
                 const float L = Lk[q * bd + tid];
                 const float lsq = L * S - Qk[q * bd + tid];
-                ga[q * bd + tid] += static_cast<double>(-lsq + Ek[q * bd + tid]);
+                atomicAdd(ga + q, static_cast<double>(-lsq + Ek[q * bd + tid]));
                 const float mus = sm[q].a.y;
                 const float a = Ck[q * bd + tid] * S - Rk[q * bd + tid];
-                gs[q * bd + tid] += static_cast<double>((mus > 0.f ? a / mus : 0.f) - (lsq + Tk[q * bd + tid]));
+                atomicAdd(gs + q, static_cast<double>((mus > 0.f ? a / mus : 0.f) - (lsq + Tk[q * bd + tid])));
             }
             active = false;
         }
     }
-    flush_tallies(B, lane, etally[tid], etally[bd + tid], c);
-    rare_flush(B);
-    // per-label gradient accumulators: warp reduction in FP64, one atomic per warp and label
-    for (int q = 0; q < K; q++) {
-        double a = ga[q * bd + tid], s = gs[q * bd + tid];
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_down_sync(kFull, a, off);
-            s += __shfl_down_sync(kFull, s, off);
-        }
-        if (lane == 0) {
-            atomicAdd(B.grad + q, a);
-            atomicAdd(B.grad + K + q, s);
+    flush_tallies(B, lane, 0.0, 0.0, c);
+    rare_flush(B);  // (its barrier also orders every lane's accumulator updates before the reads below)
+    if (threadIdx.x == 0) {
+        atomicAdd(&B.stats->total, et[0]);
+        atomicAdd(&B.stats->escape, et[1]);
+        for (int q = 0; q < K; q++) {
+            atomicAdd(B.grad + q, ga[q]);
+            atomicAdd(B.grad + K + q, gs[q]);
         }
     }
 }
