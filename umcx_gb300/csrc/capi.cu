@@ -389,9 +389,14 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         UMCX_CK(cudaMemsetAsync(ctx->counter.ptr, 0, sizeof(unsigned long long), st));
         UMCX_CK(cudaMemsetAsync(ctx->grad.ptr, 0, 2 * K * sizeof(double), st));
         const bool fp64 = s->issavevol && !(s->flags & UMCX_SIM_FP32_ACCUM);
-        if (fp64) {  // one copy: replicating the adjoint pass's volume measured no faster
-            UMCX_CK(ctx->accum64.ensure(nout * sizeof(double)));
-            UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, nout * sizeof(double), st));
+        // the FP64 volume with the copies of its hot part, as for the forward pass (accumulator_replicas)
+        const Replicas reps = fp64 ? accumulator_replicas(nvox, s->dim[3]) : Replicas{1u, 0ULL};
+        if (fp64) {
+            const size_t n64 = nout + (reps.copies - 1) * reps.len;
+            UMCX_CK(ctx->accum64.ensure(n64 * sizeof(double)));
+            UMCX_CK(cudaMemsetAsync(ctx->accum64.ptr, 0, n64 * sizeof(double), st));
+            P.rep_mask = reps.copies - 1;
+            P.rep_len = static_cast<unsigned>(reps.len);
         } else if (s->issavevol) {
             UMCX_CK(cudaMemsetAsync(ctx->fluence.ptr, 0, nout * sizeof(float), st));
         }
@@ -425,12 +430,12 @@ int umcx_gpu_forward_adjoint(umcx_context* ctx, const umcx_sim* s, const uint8_t
         UMCX_CK(cudaEventRecord(ctx->ev0, st));
         ctx->last_block = block;
         ctx->last_grid = grid;
-        launch_adjoint(grid, block, smem, s->isreflect != 0, P, B, st);
+        launch_adjoint(grid, block, smem, s->isreflect != 0, fp64 ? reps.mode(nout) : kRepNone, P, B, st);
         UMCX_CK(cudaGetLastError());
         UMCX_CK(cudaEventRecord(ctx->ev1, st));
         if (fp64) {
             launch_fp64_to_fp32(static_cast<const double*>(ctx->accum64.ptr), static_cast<float*>(ctx->fluence.ptr), nout,
-                                ctx->sm_count, st);
+                                ctx->sm_count, st, reps);
             UMCX_CK(cudaGetLastError());
         }
         umcx_result tmp;

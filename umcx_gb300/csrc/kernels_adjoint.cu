@@ -10,10 +10,16 @@ size_t adjoint_smem(const KParams& P, int block) {
            6 * K * block * sizeof(float) + block * sizeof(unsigned long long);  // + photon indices
 }
 
+template <bool R>
+static cudaError_t allow_adjoint_smem() {
+    cudaError_t e = allow_max_dynamic_smem(k_adjoint<R>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_adjoint<R, kRepPrefix>);
+    return e == cudaSuccess ? allow_max_dynamic_smem(k_adjoint<R, kRepWhole>) : e;
+}
+
 cudaError_t configure_adjoint_kernels() {
-    cudaError_t e = allow_max_dynamic_smem(k_adjoint<false>);
-    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_adjoint<true>);
-    return e;
+    cudaError_t e = allow_adjoint_smem<false>();
+    return e == cudaSuccess ? allow_adjoint_smem<true>() : e;
 }
 
 int adjoint_occupancy(bool reflect, int block, size_t smem) {
@@ -23,10 +29,18 @@ int adjoint_occupancy(bool reflect, int block, size_t smem) {
     return e == cudaSuccess ? n : 0;
 }
 
-void launch_adjoint(int grid, int block, size_t smem, bool reflect, const KParams& P, const KBuffers& B,
+template <bool R>
+static void launch_adjoint_rep(int grid, int block, size_t smem, int rep, const KParams& P, const KBuffers& B,
+                               cudaStream_t st) {
+    if (rep == kRepWhole) k_adjoint<R, kRepWhole><<<grid, block, smem, st>>>(P, B);
+    else if (rep == kRepPrefix) k_adjoint<R, kRepPrefix><<<grid, block, smem, st>>>(P, B);
+    else k_adjoint<R><<<grid, block, smem, st>>>(P, B);
+}
+
+void launch_adjoint(int grid, int block, size_t smem, bool reflect, int rep, const KParams& P, const KBuffers& B,
                     cudaStream_t st) {
-    if (reflect) k_adjoint<true><<<grid, block, smem, st>>>(P, B);
-    else k_adjoint<false><<<grid, block, smem, st>>>(P, B);
+    if (reflect) launch_adjoint_rep<true>(grid, block, smem, rep, P, B, st);
+    else launch_adjoint_rep<false>(grid, block, smem, rep, P, B, st);
 }
 
 void launch_replay(int grid, int block, bool reflect, const KParams& P, const KBuffers& B, cudaStream_t st) {

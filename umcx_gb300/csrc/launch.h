@@ -73,7 +73,7 @@ int occupancy_strict(bool reflect, bool savedet, int block, size_t smem);
 size_t adjoint_smem(const KParams& P, int block);
 cudaError_t configure_adjoint_kernels();
 int adjoint_occupancy(bool reflect, int block, size_t smem);
-void launch_adjoint(int grid, int block, size_t smem, bool reflect, const KParams& P, const KBuffers& B,
+void launch_adjoint(int grid, int block, size_t smem, bool reflect, int rep, const KParams& P, const KBuffers& B,
                     cudaStream_t st);
 void launch_replay(int grid, int block, bool reflect, const KParams& P, const KBuffers& B, cudaStream_t st);
 void launch_adjoint_reduce(const KParams& P, const DetRecord* rec, const float* ext, unsigned long long n,

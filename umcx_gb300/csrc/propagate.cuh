@@ -1131,7 +1131,8 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
 //
 // Shared memory: double ga[K], gs[K], total, escape | Medium[K] | float ppath[ppathlen][bd] |
 // float L, cnt, Q, T, E, R[K][bd] | u64 photon index[bd]
-template <bool REFLECT>
+// REP: replication mode of the FP64 output volume, as in the forward kernel
+template <bool REFLECT, int REP = kRepNone>
 __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffers B) {
     extern __shared__ double smem8[];
     const unsigned bd = blockDim.x;
@@ -1168,6 +1169,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
     cur[tid] = 0;
     Counters c;
     float S = 0.f;
+    const Replica replica = cta_replica<REP>(P);
 
     for (unsigned iter = 0;; iter++) {
         if (!active && !done) {
@@ -1212,7 +1214,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                         const int gate = deposit_gate(P, p);
                         if (gate >= 0) {
                             F = deposit_value<false>(P, p, med);
-                            deposit_add(B, p.lastvox + gate * static_cast<int>(P.dimxyz), F);
+                            deposit_add<REP>(B, p.lastvox + gate * static_cast<int>(P.dimxyz), F, replica);
                             // derivative of this deposit with respect to its own label's mua along the fixed path
                             if (P.outputtype == UMCX_OUT_ENERGY) {
                                 dF = seg * p.pw;  // d(w0 (1 - e^-mua l))/dmua = l w1
