@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define UMCX_ABI_VERSION 3
+#define UMCX_ABI_VERSION 4
 
 /* status codes */
 enum {
@@ -205,25 +205,29 @@ int umcx_gpu_backward(umcx_context* ctx, umcx_adjoint* out);
  * sizes, label counts, optics, sources and photon budgets -- run by one persistent kernel launch, replayed from a
  * CUDA graph captured at creation.  Each simulation's photons are seeded exactly as in a single run of it, so every
  * photon history, tally and output equals umcx_gpu_forward's for that simulation (up to the summation order of the
- * output volume).  Detected-photon saving is not available in batches (issavedet must be 0).
+ * output volume).  A simulation with issavedet keeps its own detected-photon records (up to its maxdetphotons
+ * rows of umcx_detp_columns(sim) floats, L164-176), from its own detectors detpos[i] ([detnum][4] {x, y, z, r};
+ * detpos, or its entry, may be NULL for simulations that save no records).
  *
- * umcx_batch_create copies the host labels (uint8 [nx][ny][nz] each) and media tables, allocates the output pool and
- * captures the graph (memsets, one or more kernel launches -- simulations are split into launches only when their
- * descriptors and optical tables exceed a CTA's shared memory -- and the FP64-to-FP32 rounding).  With labels NULL
+ * umcx_batch_create copies the host labels (uint8 [nx][ny][nz] each), media tables and detectors, allocates the
+ * output and record pools and captures the graph (memsets, one or more kernel launches -- simulations are split into
+ * launches only when their descriptors, optical and detector tables exceed a CTA's shared memory -- and the
+ * FP64-to-FP32 rounding).  With labels NULL
  * the batch's label pool starts zeroed and the caller writes each simulation's labels in place before the first run,
  * at umcx_batch_labels(b, i) (for example with umcx_gpu_build_labels, no host copy at all).
  */
 typedef struct umcx_batch umcx_batch;
 int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const uint8_t* const* labels,
-                      const float* const* media, umcx_batch** out);
+                      const float* const* media, const float* const* detpos, umcx_batch** out);
 /* Device address of simulation i's uint8 label volume inside the batch's pool (NULL on a bad index). */
 uint8_t* umcx_batch_labels(umcx_batch* b, int i);
-/* Run the whole batch once (graph launch + synchronise).  total receives the summed tallies and event counts and
- * kernel_ms the device time of the graph. */
+/* Run the whole batch once (graph launch + synchronise).  total receives the summed tallies, event counts and
+ * detections and kernel_ms the device time of the graph. */
 int umcx_batch_run(umcx_batch* b, umcx_result* total);
-/* Copy simulation i's output volume of the last run to fluence (host, [maxgate][nx][ny][nz]); res receives its
- * energy_escape / energy_total / launched (may be NULL). */
-int umcx_batch_get(umcx_batch* b, int i, float* fluence, umcx_result* res);
+/* Copy simulation i's output volume of the last run to fluence (host, [maxgate][nx][ny][nz]) and its detected-photon
+ * records to detp (host, [saved][umcx_detp_columns]); res receives its energy_escape / energy_total / launched /
+ * detected / saved.  Each of fluence, detp and res may be NULL. */
+int umcx_batch_get(umcx_batch* b, int i, float* fluence, float* detp, umcx_result* res);
 /* Re-time the batch with the given tuning (NULL: defaults) and re-capture its graph. */
 int umcx_batch_set_tuning(umcx_batch* b, const umcx_tuning* tuning);
 void umcx_batch_destroy(umcx_batch* b);

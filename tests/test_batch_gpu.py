@@ -6,6 +6,8 @@ last bits of single-precision arithmetic (the batched and single kernels are sep
 contract multiply-adds differently, so an occasional photon drifts by an ulp and then diverges): launched energy
 agrees exactly, escaped energy and output volumes to ~1e-6.  The single-run path itself is checked against the CPU
 oracle in test_forward_gpu.py."""
+import math
+
 import numpy as np
 import pytest
 
@@ -73,13 +75,130 @@ def test_zero_progress_guard_on_batched_workload(ctx):
     b.close()
 
 
-def test_batch_rejects_detectors(ctx):
+def test_batch_requires_detector_positions(ctx):
     from umcx_gb300 import Job
     from umcx_gb300.api import Batch
 
     j = Job.from_args(["--bench", "cube60b", "-n", "1000"])
-    with pytest.raises(RuntimeError, match="detected photons"):
-        Batch.from_jobs(ctx, [j])
+    assert j.sim.issavedet and j.sim.detnum > 0
+    with pytest.raises(RuntimeError, match="detpos is NULL"):
+        Batch(ctx, [j.sim], [j.labels], [j.media], None)
+
+
+def detector_rows_by_id(rows, detnum):
+    return [rows[rows[:, 0] == d] for d in range(1, detnum + 1)]
+
+
+def test_batch_detected_photons_match_single_runs(ctx):
+    """Simulations that save detected photons keep their own records inside a batch, next to simulations that save
+    none: per simulation the detection count and the per-detector record count and mean partial paths equal a single
+    run's (up to the rare photon that drifts by an ulp between the two compilations); a simulation whose row capacity
+    is below its detections counts them all and keeps exactly its capacity."""
+    from umcx_gb300 import Job
+    from umcx_gb300.api import Batch
+
+    det_jobs = [Job.from_args(["--bench", "cube60b", "-n", "40000"]),
+                Job.from_args(["--bench", "cubesph60b", "-n", "60000"]),
+                Job.from_args(["--bench", "cube60b", "-n", "30000", "-E", "7"])]
+    plain = small_batch(3, scale=0.01)
+    jobs = [plain[0], det_jobs[0], plain[1], det_jobs[1], det_jobs[2], plain[2]]
+    sims = [j.sim for j in jobs]
+    sims[4].maxdetphotons = 50  # fewer rows than detections
+    b = Batch.from_jobs(ctx, jobs, sims=sims)
+    tot = b.run()
+    assert tot.status == 0 and tot.launched == sum(s.nphoton for s in sims)
+    assert tot.detected >= tot.saved > 0
+    detected = saved = 0
+    for i, (j, s) in enumerate(zip(jobs, sims)):
+        _, r = b.get(i)
+        rows = b.detp(i)
+        detected += r.detected
+        saved += r.saved
+        if not s.issavedet:
+            assert r.detected == 0 and r.saved == 0 and rows.shape[0] == 0
+            continue
+        single = ctx.forward(s, j.labels, j.media, j.detpos)
+        n1, n2 = r.detected, single.result.detected
+        assert abs(n1 - n2) <= max(3, n2 // 500), (i, n1, n2)
+        assert r.saved == min(r.detected, s.maxdetphotons) == rows.shape[0]
+        assert rows.shape[1] == single.detp.shape[1]
+        if s.maxdetphotons < n2:
+            continue
+        assert np.all((rows[:, 0] >= 1) & (rows[:, 0] <= s.detnum))
+        for d, (a, c) in enumerate(zip(detector_rows_by_id(rows, s.detnum),
+                                       detector_rows_by_id(single.detp, s.detnum))):
+            assert abs(len(a) - len(c)) <= max(3, len(c) // 500), (i, d, len(a), len(c))
+            if len(c) > 20:
+                pa, pc = a[:, 1:1 + s.mediumnum].mean(0), c[:, 1:1 + s.mediumnum].mean(0)
+                np.testing.assert_allclose(pa, pc, rtol=2e-2, atol=1e-3 * max(1.0, float(pc.max())))
+    assert (detected, saved) == (tot.detected, tot.saved)
+    b.close()
+
+
+def test_batched_detected_photons_match_oracle(ctx):
+    """Detected-photon records of the batched kernel against the CPU oracle on the same seeds: the heterogeneous
+    60^3 + sphere geometry with reflection and 4 detectors (4e5 photons) and cube60b (2e5 photons), each entering
+    the batch as 10 photon-index ranges between simulations that save no records.  Criteria of the
+    single-simulation parity test: detection counts (in all and per detector) within 3 standard errors, every
+    per-detector mean partial path within 3 standard errors, absorbed fraction within 3 standard errors."""
+    import oracle
+    from statcheck import det_stats, run_batches, z_of_means
+
+    from umcx_gb300 import Job
+    from umcx_gb300.api import Batch
+
+    specs = [(["--bench", "cubesph60b"], 400000), (["--bench", "cube60b"], 200000)]
+    nb = 10
+    fillers = small_batch(nb * len(specs), scale=0.005)
+    entries, sims, base = [], [], []
+    for q, (args, n) in enumerate(specs):
+        j = Job.from_args([*args, "-n", str(n)])
+        base.append(j)
+        per = n // nb
+        for k in range(nb):
+            t = j.sim.copy()
+            t.photon_offset = k * per
+            t.nphoton = per
+            entries.append(j)
+            sims.append(t)
+            f = fillers[q * nb + k]
+            entries.append(f)
+            sims.append(f.sim)
+    b = Batch.from_jobs(ctx, entries, sims=sims)
+    tot = b.run()
+    assert tot.status == 0 and tot.launched == sum(s.nphoton for s in sims)
+    for q, j in enumerate(base):
+        s = j.sim
+        it = iter(range(2 * q * nb, 2 * (q + 1) * nb, 2))
+
+        def gpu(_s):
+            i = next(it)
+            flu, r = b.get(i)
+            return flu, b.detp(i), r
+
+        g = run_batches(gpu, s, nb)
+        c = run_batches(lambda _s: oracle.forward(_s, j.labels, j.media, j.detpos), s, nb)
+        za = z_of_means(g.absorbed, c.absorbed)
+        ng = sum(r.detected for r in g.results)
+        nc = sum(r.detected for r in c.results)
+        zd = (ng - nc) / math.sqrt(ng + nc)
+        line = f"{s.dim[0]}^3, {s.detnum} detectors: absorbed z={za:.2f}; detected gpu {ng} cpu {nc} z={zd:.2f}"
+        assert abs(za) < 3 and abs(zd) < 3 and ng > 100, line
+        cols = slice(1, 1 + s.mediumnum)
+        zmax = 0.0
+        for (n1, m1, s1), (n2, m2, s2) in zip(det_stats(g.detp, s.detnum, cols), det_stats(c.detp, s.detnum, cols)):
+            zn = (n1 - n2) / math.sqrt(n1 + n2) if n1 + n2 else 0.0
+            assert abs(zn) < 3, (line, n1, n2)
+            if n1 > 30 and n2 > 30:
+                z = (m1 - m2) / np.sqrt(s1 ** 2 + s2 ** 2 + 1e-30)
+                z = z[np.isfinite(z)]
+                zmax = max(zmax, float(np.abs(z).max()) if z.size else 0.0)
+                assert np.all(np.abs(z) < 3), (line, m1, m2, z)
+        print(line + f"; per-detector mean partial path max |z| {zmax:.2f}")
+    for i in range(1, len(sims), 2):  # the fillers save no records
+        _, r = b.get(i)
+        assert r.detected == 0 and b.detp(i).shape[0] == 0
+    b.close()
 
 
 def test_autotuners(ctx):

@@ -114,6 +114,8 @@ UMCX_JOB_DEVICE_LABELS = 1
 SHAPE_SPHERE, SHAPE_BOX, SHAPE_XLAYER, SHAPE_YLAYER, SHAPE_ZLAYER, SHAPE_CYLINDER = range(6)
 SHAPE_HAS_TAG, SHAPE_HAS_SIZE0, SHAPE_HAS_HI = 0x1, 0x2, 0x10
 
+ABI_VERSION = 4  # UMCX_ABI_VERSION of include/umcx_gpu.h that these signatures follow
+
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
 _U8P = C.POINTER(C.c_uint8)
@@ -133,9 +135,9 @@ SIGNATURES = [
     ("umcx_gpu_forward_adjoint", C.c_int, [_P, C.POINTER(Sim), _P, _P, _P, _P, _P, C.POINTER(Result)]),
     ("umcx_gpu_backward", C.c_int, [_P, C.POINTER(Adjoint)]),
     ("umcx_batch_create", C.c_int, [_P, C.c_int, C.POINTER(Sim), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
-                                    C.POINTER(_P)]),
+                                    C.POINTER(C.c_void_p), C.POINTER(_P)]),
     ("umcx_batch_run", C.c_int, [_P, C.POINTER(Result)]),
-    ("umcx_batch_get", C.c_int, [_P, C.c_int, _P, C.POINTER(Result)]),
+    ("umcx_batch_get", C.c_int, [_P, C.c_int, _P, _P, C.POINTER(Result)]),
     ("umcx_batch_set_tuning", C.c_int, [_P, C.POINTER(Tuning)]),
     ("umcx_batch_destroy", None, [_P]),
     ("umcx_batch_labels", C.c_void_p, [_P, C.c_int]),
@@ -184,6 +186,8 @@ def load() -> C.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.umcx_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{LIB_PATH} has ABI {lib.umcx_abi_version()}, these bindings {ABI_VERSION}: rebuild it")
         _lib = lib
     return _lib
 

@@ -336,18 +336,24 @@ class Context:
 class Batch:
     """Many independent simulations in one persistent, graph-captured launch (umcx_batch_*)."""
 
-    def __init__(self, ctx: Context, sims, labels, media):
-        """labels: one host uint8 volume per simulation, or None to write them in place afterwards (label_ptr)."""
+    def __init__(self, ctx: Context, sims, labels, media, detpos=None):
+        """labels: one host uint8 volume per simulation, or None to write them in place afterwards (label_ptr).
+        detpos: per simulation its detectors ([detnum, 4] {x, y, z, r}) or None; needed by the simulations that
+        save detected photons (issavedet)."""
         lib = load()
         n = len(sims)
         arr = (Sim * n)(*[s.copy() for s in sims])
         keep_lab = [] if labels is None else [np.ascontiguousarray(x, np.uint8) for x in labels]
         keep_med = [np.ascontiguousarray(m, np.float32) for m in media]
+        keep_det = [None if d is None or len(d) == 0 else np.ascontiguousarray(d, np.float32)
+                    for d in (detpos if detpos is not None else [None] * n)]
         lab = None if labels is None else (C.c_void_p * n)(*[x.ctypes.data for x in keep_lab])
         med = (C.c_void_p * n)(*[m.ctypes.data for m in keep_med])
+        det = (C.c_void_p * n)(*[None if d is None else d.ctypes.data for d in keep_det])
         self._ctx = ctx
         self._h = C.c_void_p()
-        check(lib.umcx_batch_create(ctx.handle, n, arr, lab, med, C.byref(self._h)), ctx.handle, "umcx_batch_create")
+        check(lib.umcx_batch_create(ctx.handle, n, arr, lab, med, det, C.byref(self._h)), ctx.handle,
+              "umcx_batch_create")
         self.sims = [s.copy() for s in sims]
 
     @classmethod
@@ -356,9 +362,10 @@ class Batch:
         device_labels=True builds every label volume on the GPU straight into the batch's label pool
         (umcx_job_build_labels at umcx_batch_labels), with no host volume at all."""
         sims = [j.sim for j in jobs] if sims is None else sims
+        detpos = [j.detpos for j in jobs]
         if not device_labels:
-            return cls(ctx, sims, [j.labels for j in jobs], [j.media for j in jobs])
-        b = cls(ctx, sims, None, [j.media for j in jobs])
+            return cls(ctx, sims, [j.labels for j in jobs], [j.media for j in jobs], detpos)
+        b = cls(ctx, sims, None, [j.media for j in jobs], detpos)
         for i, j in enumerate(jobs):
             j.build_labels(ctx, b.label_ptr(i))
         return b
@@ -387,11 +394,23 @@ class Batch:
             if flu.dtype != np.float32 or flu.size < n or not flu.flags.c_contiguous:
                 raise ValueError("out must be a contiguous float32 array of nx*ny*nz*maxgate elements")
         r = Result()
-        check(load().umcx_batch_get(self._h, int(i), None if flu is None else flu.ctypes.data, C.byref(r)),
+        check(load().umcx_batch_get(self._h, int(i), None if flu is None else flu.ctypes.data, None, C.byref(r)),
               self._ctx.handle, "umcx_batch_get")
         if flu is not None:
             flu = flu.reshape(s.dim[3], s.dim[0], s.dim[1], s.dim[2])
         return flu, r
+
+    def detp(self, i: int) -> np.ndarray:
+        """Simulation i's detected-photon records of the last run, [saved, umcx_detp_columns] (L164-176)."""
+        lib = load()
+        r = Result()
+        check(lib.umcx_batch_get(self._h, int(i), None, None, C.byref(r)), self._ctx.handle, "umcx_batch_get")
+        cols = lib.umcx_detp_columns(C.byref(self.sims[i]))
+        rows = np.zeros((int(r.saved), cols), np.float32)
+        if rows.size:
+            check(lib.umcx_batch_get(self._h, int(i), None, rows.ctypes.data, None), self._ctx.handle,
+                  "umcx_batch_get")
+        return rows
 
     def set_tuning(self, block_size: int = 0, blocks_per_sm: int = 0, aggregation: int = 0, budget_ms: int = 0):
         t = Tuning(block_size, blocks_per_sm, aggregation, budget_ms)

@@ -38,6 +38,7 @@ CU_UNITS = {
     "kernels_strict.cu": ["--fmad=false"],
     "kernels_adjoint.cu": FAST,
     "kernels_batch.cu": FAST,
+    "kernels_batch_det.cu": FAST,
     "peaks.cu": [],
     "noalloc.cu": [],
     "raster.cu": [],

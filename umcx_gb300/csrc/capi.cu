@@ -687,21 +687,24 @@ struct umcx_batch {
     umcx_context* ctx = nullptr;
     int nsim = 0;
     std::vector<umcx_sim> sims;
-    std::vector<unsigned long long> out_off, label_off;
-    unsigned long long nout_total = 0, lab_total = 0;
+    std::vector<unsigned long long> out_off, label_off, detp_off;
+    unsigned long long nout_total = 0, lab_total = 0, ndetp_total = 0;
     bool reflect = false, fp64 = true;
     struct Chunk {
         int first = 0, count = 0, media_first = 0, total_media = 0;
+        int det_first = 0, total_det = 0, ppathlen = 0;  // detectors and partial-path slots of its simulations
+        bool savedet = false;                             // some simulation of the chunk saves detected photons
         unsigned long long photons = 0, begin_off = 0;
         int block = 0, grid = 0;
         size_t smem = 0;
     };
     std::vector<Chunk> chunks;
     std::vector<SimDesc> descs;
-    DevBuf labels, media, d_descs, d_begin, tallies, out32, out64, counters, stats;
+    DevBuf labels, media, dets, d_descs, d_begin, tallies, out32, out64, detp, detected, counters, stats;
     cudaGraphExec_t exec = nullptr;
     umcx_tuning tuning{};
     std::vector<double> host_tallies;
+    std::vector<unsigned long long> host_detected;
 };
 
 namespace {
@@ -711,9 +714,9 @@ constexpr size_t kBatchSmemBudget = 200 * 1024;
 void batch_plan(umcx_batch* b) {
     for (auto& ch : b->chunks) {
         const int block = b->tuning.block_size > 0 ? b->tuning.block_size : 512;
-        const size_t smem = batch_smem(ch.count, ch.total_media, block);
+        const size_t smem = batch_smem(ch.count, ch.total_media, ch.total_det, ch.ppathlen, block);
         if (smem > kMaxDynamicSmem) throw InputError("batch chunk does not fit shared memory at this block size");
-        int occ = batch_occupancy(b->reflect, block, smem);
+        int occ = batch_occupancy(b->reflect, ch.savedet, block, smem);
         if (occ < 1) occ = 1;
         const int per_sm = b->tuning.blocks_per_sm > 0 ? std::min(b->tuning.blocks_per_sm, occ) : occ;
         int grid = b->ctx->sm_count * per_sm;
@@ -730,6 +733,7 @@ void batch_enqueue(umcx_batch* b, cudaStream_t st) {
     UMCX_CK(cudaMemsetAsync(b->stats.ptr, 0, sizeof(KStats), st));
     UMCX_CK(cudaMemsetAsync(b->counters.ptr, 0, sizeof(unsigned long long) * b->chunks.size(), st));
     UMCX_CK(cudaMemsetAsync(b->tallies.ptr, 0, sizeof(double) * 2 * b->nsim, st));
+    UMCX_CK(cudaMemsetAsync(b->detected.ptr, 0, sizeof(unsigned long long) * b->nsim, st));
     if (b->fp64) UMCX_CK(cudaMemsetAsync(b->out64.ptr, 0, sizeof(double) * b->nout_total, st));
     else UMCX_CK(cudaMemsetAsync(b->out32.ptr, 0, sizeof(float) * b->nout_total, st));
     for (size_t c = 0; c < b->chunks.size(); c++) {
@@ -739,8 +743,13 @@ void batch_enqueue(umcx_batch* b, cudaStream_t st) {
         bp.sims = static_cast<const SimDesc*>(b->d_descs.ptr) + ch.first;
         bp.begin = static_cast<const unsigned long long*>(b->d_begin.ptr) + ch.begin_off;
         bp.tallies = static_cast<double*>(b->tallies.ptr) + 2 * ch.first;
+        bp.dets = ch.total_det ? static_cast<const float4*>(b->dets.ptr) + ch.det_first : nullptr;
+        bp.detected = static_cast<unsigned long long*>(b->detected.ptr) + ch.first;
         bp.nsim = ch.count;
         bp.total_media = ch.total_media;
+        bp.total_det = ch.total_det;
+        bp.ppathlen = ch.ppathlen;
+        bp.savedet = ch.savedet ? 1 : 0;
         bp.aggregate = b->tuning.aggregation == 2 ? 1 : 0;
         bp.total = ch.photons;
         bp.budget_ns = b->tuning.budget_ms > 0 ? static_cast<unsigned long long>(b->tuning.budget_ms) * 1000000ULL
@@ -750,7 +759,8 @@ void batch_enqueue(umcx_batch* b, cudaStream_t st) {
         B.labels = static_cast<const uint8_t*>(b->labels.ptr);
         B.fluence = static_cast<float*>(b->out32.ptr);
         B.fluence64 = b->fp64 ? static_cast<double*>(b->out64.ptr) : nullptr;
-        set_extents(B, b->lab_total, b->nout_total, 0, 0);
+        B.detp = ch.savedet ? static_cast<float*>(b->detp.ptr) : nullptr;  // NULL when no simulation keeps rows
+        set_extents(B, b->lab_total, b->nout_total, ch.savedet ? b->ndetp_total : 0, 0);
         B.media = static_cast<const Medium*>(b->media.ptr) + ch.media_first;
         B.stats = static_cast<KStats*>(b->stats.ptr);
         B.counter = static_cast<unsigned long long*>(b->counters.ptr) + c;
@@ -787,7 +797,8 @@ void batch_capture(umcx_batch* b) {
     UMCX_CK(e);
 }
 
-SimDesc make_desc(const umcx_sim* s, unsigned media_base, unsigned long long label_off, unsigned long long out_off) {
+SimDesc make_desc(const umcx_sim* s, unsigned media_base, unsigned det_base, unsigned long long label_off,
+                  unsigned long long out_off, unsigned long long detp_off) {
     const KParams P = make_params(s, nullptr);
     SimDesc d;
     std::memset(&d, 0, sizeof(d));
@@ -801,7 +812,7 @@ SimDesc make_desc(const umcx_sim* s, unsigned media_base, unsigned long long lab
     d.issavevol = P.issavevol;
     d.outputtype = P.outputtype;
     d.srctype = P.srctype;
-    d.pad = 0;
+    d.det_base = det_base;
     d.media_base = media_base;
     d.tstart = P.tstart;
     d.tend = P.tend;
@@ -817,6 +828,12 @@ SimDesc make_desc(const umcx_sim* s, unsigned media_base, unsigned long long lab
     d.srcrdir = P.srcrdir;
     d.srcparam1 = P.srcparam1;
     d.srcparam2 = P.srcparam2;
+    d.detnum = s->issavedet ? s->detnum : 0;
+    d.savedetflag = P.savedetflag;
+    d.ppathlen = P.ppathlen;
+    d.cols = P.cols;
+    d.maxdetphotons = P.maxdetphotons;
+    d.detp_off = detp_off;
     return d;
 }
 
@@ -843,7 +860,7 @@ void batch_upload_begin(umcx_batch* b, const std::vector<unsigned long long>& co
 extern "C" {
 
 int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const uint8_t* const* labels,
-                      const float* const* media, umcx_batch** out) {
+                      const float* const* media, const float* const* detpos, umcx_batch** out) {
     if (!ctx || !out) return UMCX_ERR_INPUT;
     *out = nullptr;
     umcx_batch* b = new (std::nothrow) umcx_batch();
@@ -856,15 +873,26 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
         b->nsim = nsim;
         b->sims.assign(sims, sims + nsim);
         std::vector<Medium> table;
-        std::vector<unsigned long long> label_off(static_cast<size_t>(nsim)), media_first(static_cast<size_t>(nsim));
+        std::vector<float4> dtable;
+        std::vector<unsigned long long> label_off(static_cast<size_t>(nsim)), media_first(static_cast<size_t>(nsim)),
+            det_first(static_cast<size_t>(nsim));
         unsigned long long lab_total = 0;
         b->out_off.resize(static_cast<size_t>(nsim));
+        b->detp_off.resize(static_cast<size_t>(nsim));
         b->fp64 = false;
         for (int i = 0; i < nsim; i++) {
             const umcx_sim* s = &sims[i];
             validate(s);
-            if (s->issavedet) throw InputError("simulation " + std::to_string(i) + ": batches do not save detected photons");
             if (s->flags & UMCX_SIM_STRICT_MATH) throw InputError("batches run the fast-math kernel only");
+            det_first[static_cast<size_t>(i)] = dtable.size();
+            b->detp_off[static_cast<size_t>(i)] = b->ndetp_total;
+            if (s->issavedet) {  // its detectors into the batch's table, its rows into the record pool
+                if (s->detnum > 0 && (!detpos || !detpos[i]))
+                    throw InputError("simulation " + std::to_string(i) + ": detpos is NULL but detnum > 0");
+                const KParams P = make_params(s, detpos ? detpos[i] : nullptr);
+                for (int d = 0; d < s->detnum; d++) dtable.push_back(P.det[d]);
+                b->ndetp_total += static_cast<unsigned long long>(P.maxdetphotons) * static_cast<unsigned>(P.cols);
+            }
             if ((labels && !labels[i]) || !media[i])
                 throw InputError("simulation " + std::to_string(i) + ": NULL labels or media");
             const unsigned long long nvox = 1ULL * s->dim[0] * s->dim[1] * s->dim[2];
@@ -883,25 +911,36 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
             umcx_batch::Chunk ch;
             ch.first = first;
             ch.media_first = static_cast<int>(media_first[static_cast<size_t>(first)]);
-            int count = 0, tm = 0;
+            ch.det_first = static_cast<int>(det_first[static_cast<size_t>(first)]);
+            int count = 0, tm = 0, td = 0, pp = 0;
             while (first + count < nsim) {
-                const int m = sims[first + count].mediumnum;
-                if (count > 0 && batch_smem(count + 1, tm + m, 1024) > kBatchSmemBudget) break;
-                tm += m;
+                const umcx_sim& s = sims[first + count];
+                const int dn = s.issavedet ? s.detnum : 0;
+                const int pl = make_params(&s, nullptr).ppathlen;
+                if (count > 0 && batch_smem(count + 1, tm + s.mediumnum, td + dn, std::max(pp, pl), 1024) > kBatchSmemBudget)
+                    break;
+                tm += s.mediumnum;
+                td += dn;
+                pp = std::max(pp, pl);
+                if (s.issavedet) ch.savedet = true;
                 count++;
             }
             ch.count = count;
             ch.total_media = tm;
+            ch.total_det = td;
+            ch.ppathlen = pp;
             b->chunks.push_back(ch);
             first += count;
         }
-        // descriptors (media_base relative to the chunk's first medium)
+        // descriptors (media_base and det_base relative to the chunk's first medium and detector)
         b->descs.resize(static_cast<size_t>(nsim));
         for (auto& ch : b->chunks)
-            for (int i = ch.first; i < ch.first + ch.count; i++)
-                b->descs[static_cast<size_t>(i)] =
-                    make_desc(&sims[i], static_cast<unsigned>(media_first[static_cast<size_t>(i)] - ch.media_first),
-                              label_off[static_cast<size_t>(i)], b->out_off[static_cast<size_t>(i)]);
+            for (int i = ch.first; i < ch.first + ch.count; i++) {
+                const size_t k = static_cast<size_t>(i);
+                b->descs[k] = make_desc(&sims[i], static_cast<unsigned>(media_first[k] - ch.media_first),
+                                        static_cast<unsigned>(det_first[k] - ch.det_first), label_off[k],
+                                        b->out_off[k], b->detp_off[k]);
+            }
         std::vector<unsigned long long> counts(static_cast<size_t>(nsim)), totals;
         for (int i = 0; i < nsim; i++) counts[static_cast<size_t>(i)] = sims[i].nphoton;
         unsigned long long boff = 0;
@@ -925,6 +964,12 @@ int umcx_batch_create(umcx_context* ctx, int nsim, const umcx_sim* sims, const u
         UMCX_CK(cudaMemcpy(b->media.ptr, table.data(), table.size() * sizeof(Medium), cudaMemcpyHostToDevice));
         UMCX_CK(b->d_descs.ensure(b->descs.size() * sizeof(SimDesc)));
         UMCX_CK(cudaMemcpy(b->d_descs.ptr, b->descs.data(), b->descs.size() * sizeof(SimDesc), cudaMemcpyHostToDevice));
+        if (!dtable.empty()) {
+            UMCX_CK(b->dets.ensure(dtable.size() * sizeof(float4)));
+            UMCX_CK(cudaMemcpy(b->dets.ptr, dtable.data(), dtable.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        }
+        if (b->ndetp_total) UMCX_CK(b->detp.ensure(sizeof(float) * b->ndetp_total));
+        UMCX_CK(b->detected.ensure(sizeof(unsigned long long) * nsim));
         UMCX_CK(b->tallies.ensure(sizeof(double) * 2 * nsim));
         UMCX_CK(b->out32.ensure(sizeof(float) * (b->nout_total ? b->nout_total : 1)));
         if (b->fp64) UMCX_CK(b->out64.ensure(sizeof(double) * (b->nout_total ? b->nout_total : 1)));
@@ -957,14 +1002,20 @@ int umcx_batch_run(umcx_batch* b, umcx_result* total) {
         UMCX_CK(cudaMemcpyAsync(&stats, b->stats.ptr, sizeof(stats), cudaMemcpyDeviceToHost, st));
         UMCX_CK(cudaMemcpyAsync(b->host_tallies.data(), b->tallies.ptr, sizeof(double) * 2 * b->nsim,
                                 cudaMemcpyDeviceToHost, st));
+        b->host_detected.resize(static_cast<size_t>(b->nsim));
+        UMCX_CK(cudaMemcpyAsync(b->host_detected.data(), b->detected.ptr, sizeof(unsigned long long) * b->nsim,
+                                cudaMemcpyDeviceToHost, st));
         UMCX_CK(cudaStreamSynchronize(st));
         float ms = 0.f;
         UMCX_CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         if (total) {
             std::memset(total, 0, sizeof(*total));
             for (int i = 0; i < b->nsim; i++) {
-                total->energy_escape += b->host_tallies[static_cast<size_t>(2 * i)];
-                total->energy_total += b->host_tallies[static_cast<size_t>(2 * i + 1)];
+                const size_t k = static_cast<size_t>(i);
+                total->energy_escape += b->host_tallies[2 * k];
+                total->energy_total += b->host_tallies[2 * k + 1];
+                total->detected += b->host_detected[k];
+                total->saved += std::min<unsigned long long>(b->host_detected[k], b->descs[k].maxdetphotons);
             }
             total->launched = stats.launched;
             total->steps = stats.steps;
@@ -986,7 +1037,7 @@ int umcx_batch_run(umcx_batch* b, umcx_result* total) {
     return rc;
 }
 
-int umcx_batch_get(umcx_batch* b, int i, float* fluence, umcx_result* res) {
+int umcx_batch_get(umcx_batch* b, int i, float* fluence, float* detp, umcx_result* res) {
     if (!b) return UMCX_ERR_INPUT;
     return guarded(b->ctx, [&]() {
         if (i < 0 || i >= b->nsim) throw InputError("simulation index out of range");
@@ -997,6 +1048,13 @@ int umcx_batch_get(umcx_batch* b, int i, float* fluence, umcx_result* res) {
             UMCX_CK(cudaMemcpy(fluence, static_cast<float*>(b->out32.ptr) + b->out_off[static_cast<size_t>(i)],
                                n * sizeof(float), cudaMemcpyDeviceToHost));
         }
+        const SimDesc& d = b->descs[static_cast<size_t>(i)];
+        const unsigned long long detected =
+            b->host_detected.size() == static_cast<size_t>(b->nsim) ? b->host_detected[static_cast<size_t>(i)] : 0ULL;
+        const unsigned long long saved = std::min<unsigned long long>(detected, d.maxdetphotons);
+        if (detp && saved)
+            UMCX_CK(cudaMemcpy(detp, static_cast<float*>(b->detp.ptr) + d.detp_off,
+                               saved * static_cast<unsigned>(d.cols) * sizeof(float), cudaMemcpyDeviceToHost));
         if (res) {
             std::memset(res, 0, sizeof(*res));
             if (b->host_tallies.size() == static_cast<size_t>(2 * b->nsim)) {
@@ -1004,6 +1062,8 @@ int umcx_batch_get(umcx_batch* b, int i, float* fluence, umcx_result* res) {
                 res->energy_total = b->host_tallies[static_cast<size_t>(2 * i + 1)];
             }
             res->launched = s.nphoton;
+            res->detected = detected;
+            res->saved = saved;
         }
         return UMCX_OK;
     });
@@ -1034,6 +1094,9 @@ void umcx_batch_destroy(umcx_batch* b) {
     b->d_descs.release();
     b->d_begin.release();
     b->tallies.release();
+    b->dets.release();
+    b->detp.release();
+    b->detected.release();
     b->out32.release();
     b->out64.release();
     b->counters.release();

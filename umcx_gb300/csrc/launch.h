@@ -80,12 +80,17 @@ void launch_adjoint_reduce(const KParams& P, const DetRecord* rec, const float* 
                            const Medium* media, double* read, double* gmua, double* gmus, int sm_count,
                            cudaStream_t st);
 
-// batched simulations (kernels_batch.cu)
-size_t batch_smem(int nsim, int total_media, int block);
+// batched simulations (kernels_batch.cu; the instances that save detected photons in kernels_batch_det.cu).
+// launch_batch runs the record-saving kernel when BP.savedet is set.
+size_t batch_smem(int nsim, int total_media, int total_det, int ppathlen, int block);
 cudaError_t configure_batch_kernels();
-int batch_occupancy(bool reflect, int block, size_t smem);
+int batch_occupancy(bool reflect, bool savedet, int block, size_t smem);
 void launch_batch(int grid, int block, size_t smem, bool reflect, const BParams& BP, const KBuffers& B,
                   cudaStream_t st);
+cudaError_t configure_batch_det_kernels();
+int batch_det_occupancy(bool reflect, int block, size_t smem);
+void launch_batch_det(int grid, int block, size_t smem, bool reflect, const BParams& BP, const KBuffers& B,
+                      cudaStream_t st);
 
 // device label builder (raster.cu): one detector's half-voxel sampling lattice, coordinates at coords[off + i]
 struct DetLattice {

@@ -44,7 +44,8 @@ inline Medium make_medium(const float* m, int outputtype) {
     return r;
 }
 
-// kernel parameters of a checked simulation description; detpos holds detnum {x, y, z, r} rows
+// kernel parameters of a checked simulation description; detpos holds detnum {x, y, z, r} rows (NULL: no
+// detector table, for callers that stage detectors elsewhere)
 inline KParams make_params(const umcx_sim* s, const float* detpos) {
     KParams P;
     std::memset(&P, 0, sizeof(P));
@@ -63,7 +64,9 @@ inline KParams make_params(const umcx_sim* s, const float* detpos) {
     P.isreflect = s->isreflect;
     P.issavevol = s->issavevol;
     P.issavedet = s->issavedet;
-    P.savedetflag = s->savedetflag;
+    // a simulation that saves no records has no record fields: the kernels that keep partial paths for several
+    // simulations at once (the batch) test only savedetflag, and size the per-lane slots by ppathlen
+    P.savedetflag = s->issavedet ? s->savedetflag : 0;
     P.mediumnum = s->mediumnum;
     P.outputtype = s->outputtype;
     P.detnum = s->detnum;
@@ -78,7 +81,7 @@ inline KParams make_params(const umcx_sim* s, const float* detpos) {
     P.srcparam1 = make_float4(s->srcparam1[0], s->srcparam1[1], s->srcparam1[2], s->srcparam1[3]);
     P.srcparam2 = make_float4(s->srcparam2[0], s->srcparam2[1], s->srcparam2[2], s->srcparam2[3]);
     P.budget_ns = kDefaultBudgetNs;
-    for (int d = 0; d < s->detnum; d++)
+    for (int d = 0; detpos && d < s->detnum; d++)
         P.det[d] = make_float4(detpos[4 * d], detpos[4 * d + 1], detpos[4 * d + 2], detpos[4 * d + 3]);
     return P;
 }

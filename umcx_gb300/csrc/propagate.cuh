@@ -854,13 +854,16 @@ __device__ __forceinline__ void append_detected(const KParams& P, const KBuffers
     }
 }
 
-// the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction]
-__device__ __forceinline__ void write_detp(const KParams& P, const KBuffers& B, const Photon& p, const float* ppath,
-                                           unsigned stride, int d, unsigned long long slot) {
-    if (!index_ok(&B.stats->error, (slot + 1) * static_cast<unsigned long long>(P.cols), UMCX_EXTENT(B, n_detp) + 1,
-                  kSiteDetRow))
+// the standard record of L171-174: [detid][ppath x ppathlen][exit position][exit direction], in row `slot` of the
+// record array that starts `base` floats into B.detp (0 for a single simulation; the simulation's offset in a batch)
+template <class PV>
+__device__ __forceinline__ void write_detp(const PV& P, const KBuffers& B, const Photon& p, const float* ppath,
+                                           unsigned stride, int d, unsigned long long slot,
+                                           unsigned long long base = 0) {
+    if (!index_ok(&B.stats->error, base + (slot + 1) * static_cast<unsigned long long>(P.cols),
+                  UMCX_EXTENT(B, n_detp) + 1, kSiteDetRow))
         return;
-    float* rec = B.detp + slot * static_cast<unsigned long long>(P.cols);
+    float* rec = B.detp + base + slot * static_cast<unsigned long long>(P.cols);
     int k = 0;
     if (P.savedetflag & UMCX_DET_ID) rec[k++] = static_cast<float>(d + 1);
     if (P.savedetflag & UMCX_DET_PPATH)
@@ -1359,13 +1362,13 @@ __global__ void __launch_bounds__(1024) k_replay(const KParams P, const KBuffers
 }
 
 // =============================================================================================== batched kernel
-// One simulation of a batch (192 bytes, staged in shared memory).  Member names match KParams so the engine
-// functions (launch, step, advance, ...) take either.
+// One simulation of a batch (224 bytes, staged in shared memory).  Member names match KParams so the engine
+// functions (launch, step, advance, write_detp, ...) take either.
 struct SimDesc {
     int nx, ny, nz, maxgate;
     unsigned dimyz, dimxyz;
     int isreflect, issavevol, outputtype, srctype;
-    unsigned pad, media_base;       // media_base: first Medium of this simulation in the batch's table
+    unsigned det_base, media_base;  // first detector / Medium of this simulation in the batch's tables
     float tstart, tend, rtstep, unitinmm;
     unsigned seeds[4];
     unsigned long long label_off;      // byte offset of its labels in the label pool
@@ -1373,14 +1376,22 @@ struct SimDesc {
     unsigned long long photon_offset;  // photon index of its first photon (seeds photon i as in a single run)
     unsigned long long nphoton;
     float4 srcpos, srcdir, srcrdir, srcparam1, srcparam2;
+    // detected-photon records (L164-176, L429-435); detnum is 0 for a simulation that saves none
+    int detnum, savedetflag, ppathlen, cols;
+    unsigned long long maxdetphotons;  // rows reserved for it in the record pool
+    unsigned long long detp_off;       // float offset of its first row in the record pool
 };
-static_assert(sizeof(SimDesc) == 192, "SimDesc layout");
+static_assert(sizeof(SimDesc) == 224, "SimDesc layout");
 
 struct BParams {
     const SimDesc* sims;              // [nsim]
     const unsigned long long* begin;  // [nsim + 1]: prefix sums of photon counts (batch photon index space)
     double* tallies;                  // [nsim][2]: escape, total (L765-770) per simulation
-    int nsim, total_media, aggregate, pad;
+    const float4* dets;               // [total_det]: detectors {x, y, z, r} of the simulations that save records
+    unsigned long long* detected;     // [nsim]: detections per simulation, including those beyond its row capacity
+    int nsim, total_media, aggregate, total_det;
+    int ppathlen;                     // largest ppathlen of the simulations (per-lane partial-path slots)
+    int savedet;                      // some simulation saves detected photons: the SAVEDET instance runs
     unsigned long long total;         // photons in the whole batch
     unsigned long long budget_ns;
 };
@@ -1396,24 +1407,31 @@ __device__ __forceinline__ void deposit_add64(const KBuffers& B, long long idx, 
 // search over the prefix sums names the simulation, whose descriptor and optical table sit in shared memory.
 // Consecutive indices belong to the same simulation, so at any moment only one or two simulations are in flight and
 // their outputs stay in L2, while the tail of one simulation overlaps the start of the next.
-// Shared memory: SimDesc[nsim] | u64 begin[nsim + 1] (padded to 16 B) | Medium[total_media] | float aggbuf[blockDim] |
-// double escape, total[blockDim]
-template <bool REFLECT, bool AGG = false>
+// SAVEDET: detected-photon records of the simulations that save them (a detection takes its row with one atomic on
+// the simulation's counter: lanes of one warp can end photons of different simulations, and detections are rare).
+// Shared memory: SimDesc[nsim] | u64 begin[nsim + 1] (padded to 16 B) | Medium[total_media] | float4 det[total_det] |
+// float aggbuf[blockDim] | double escape, total[blockDim] | float ppath[ppathlen][blockDim]
+template <bool REFLECT, bool AGG = false, bool SAVEDET = false>
 __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers B) {
     extern __shared__ float4 smem4[];
     SimDesc* sd = reinterpret_cast<SimDesc*>(smem4);
     unsigned long long* begin = reinterpret_cast<unsigned long long*>(sd + BP.nsim);
     Medium* sm = reinterpret_cast<Medium*>(begin + ((BP.nsim + 2) & ~1));
-    float* aggbuf = reinterpret_cast<float*>(sm + BP.total_media);
+    float4* sdet = reinterpret_cast<float4*>(sm + BP.total_media);
+    float* aggbuf = reinterpret_cast<float*>(sdet + (SAVEDET ? BP.total_det : 0));
     double* etally = reinterpret_cast<double*>(aggbuf + blockDim.x);  // [2][blockDim]: escape, total of `tally_sim`
+    float* ppath = reinterpret_cast<float*>(etally + 2 * blockDim.x);  // [ppathlen][blockDim] (SAVEDET)
     {
+        constexpr int kDescVec = sizeof(SimDesc) / sizeof(float4);
         const float4* s = reinterpret_cast<const float4*>(BP.sims);
         float4* d = reinterpret_cast<float4*>(sd);
-        for (int k = threadIdx.x; k < BP.nsim * 12; k += blockDim.x) d[k] = s[k];
+        for (int k = threadIdx.x; k < BP.nsim * kDescVec; k += blockDim.x) d[k] = s[k];
         for (int k = threadIdx.x; k <= BP.nsim; k += blockDim.x) begin[k] = BP.begin[k];
         const float4* ms = reinterpret_cast<const float4*>(B.media);
         float4* md = reinterpret_cast<float4*>(sm);
         for (int k = threadIdx.x; k < 3 * BP.total_media; k += blockDim.x) md[k] = ms[k];
+        if (SAVEDET)
+            for (int k = threadIdx.x; k < BP.total_det; k += blockDim.x) sdet[k] = BP.dets[k];
     }
     rare_reset();
     set_deadline(BP.budget_ns);
@@ -1459,6 +1477,8 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 rare_count(kRareLaunch);
                 const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
                 active = start_photon<false>(S, lab, p, S.photon_offset + (g - begin[sim]));
+                if (SAVEDET && active)
+                    for (int q = 0; q < S.ppathlen; q++) ppath[q * blockDim.x + tid] = 0.f;
             }
         }
         // warp-uniform exits, tested every 16 iterations (a finished lane idles for at most 15 more)
@@ -1477,6 +1497,9 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 const SimDesc& S = sd[sim];
                 const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
                 advance<false, REFLECT, false>(S, lab, sm + S.media_base, p, ev, c);
+                if (SAVEDET && (S.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0 &&
+                    index_ok(&B.stats->error, ev.left_mid - 1u, static_cast<unsigned>(S.ppathlen), kSitePath))
+                    ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
                 const bool dep = ev.crossed && S.issavevol && ev.gate >= 0;
                 dep_idx = dep ? static_cast<long long>(S.out_off) + ev.left_vox +
                                     static_cast<long long>(ev.gate) * static_cast<long long>(S.dimxyz)
@@ -1505,7 +1528,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
             term = photon_step<false, REFLECT, false>(
                 S, lab, sm + S.media_base, p, c,
                 [&](unsigned mid, const Medium& m) {
-                    record_crossing<false, false>(S, p, mid, m, nullptr, &B.stats->error, [&](int vox, int gate, float v) {
+                    record_crossing<false, SAVEDET>(S, p, mid, m, ppath + tid, &B.stats->error, [&](int vox, int gate, float v) {
                         deposit_add64(B, static_cast<long long>(S.out_off) + vox + static_cast<long long>(gate) * S.dimxyz,
                                       v);
                     });
@@ -1515,6 +1538,15 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
         if (term) {
             count_stopped(p);
             if (!AGG) c.steps += p.nsteps;  // photon_step does not count steps one by one
+            if (SAVEDET) {
+                const SimDesc& S = sd[sim];
+                if ((p.media & UMCX_LABEL_DET) && p.ly <= S.tend)  // L276-278, L429-435
+                    for (int d = 0; d < S.detnum; d++) {
+                        if (!det_hit(sdet[S.det_base + d], p)) continue;
+                        const unsigned long long slot = atomicAdd(BP.detected + sim, 1ULL);
+                        if (slot < S.maxdetphotons) write_detp(S, B, p, ppath + tid, blockDim.x, d, slot, S.detp_off);
+                    }
+            }
             if ((p.media & UMCX_LABEL_MASK) != 0u) {
                 etally[blockDim.x + tid] += p.launchw;
                 etally[tid] += p.pw;
