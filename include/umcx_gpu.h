@@ -294,12 +294,12 @@ int umcx_gpu_rng_dump(umcx_context* ctx, const uint32_t seeds[4], uint64_t photo
  * (photon counter, tallies, optical table) lives in one fixed device array of UMCX_NOALLOC_SCRATCH_BYTES inside the
  * library, held by every GPU that loads it until the process exits; at most UMCX_NOALLOC_MAX_MEDIA media fit, and
  * larger tables are rejected with UMCX_ERR_INPUT.  The output volume is accumulated in FP32 directly in d_fluence
- * (as with UMCX_SIM_FP32_ACCUM).  The first call on a device looks up that array's address; make it before any
- * stream capture.  That address belongs to the device's primary context, so after the application resets the
- * device (cudaDeviceReset) this entry point must not be called again in the process.  Each call synchronises its
- * stream before returning (it reads the tallies back).  All calls share the array: calls whose GPU work overlaps
- * race and must be serialised by the caller.  Inputs are checked by the same rules as umcx_gpu_forward_device.
- * res->kernel_ms is 0 (no events).
+ * (as with UMCX_SIM_FP32_ACCUM).  Each call is synchronous: it reads the tallies back and synchronises its stream
+ * before returning, so it cannot be recorded into a CUDA graph (stream capture).  The array's address belongs to
+ * the device's primary context, so after the application resets the device (cudaDeviceReset) this entry point must
+ * not be called again in the process.  All calls share the array: calls whose GPU work overlaps race and must be
+ * serialised by the caller.  Inputs are checked by the same rules as umcx_gpu_forward_device.  res->kernel_ms is 0
+ * (no events).
  */
 #define UMCX_NOALLOC_SCRATCH_BYTES 8192
 #define UMCX_NOALLOC_MAX_MEDIA 128

@@ -9,12 +9,13 @@
 //
 // The array is a static __device__ object: every GPU that loads this library holds it (SCRATCH_BYTES) until the
 // process exits.  Host code cannot use its name as an address, so the first call on each device looks the address
-// up with cudaGetSymbolAddress (with that device current) and caches it; make that first call before any stream
-// capture.  The cached address belongs to the device's primary context: after a cudaDeviceReset by the host
-// application the entry point must not be called again in that process.  Every call synchronises its stream before
-// it returns (it reads the tallies back).  All calls share the array and it keeps the last call's contents, so
-// each call clears the counter and tallies before its launch.  Calls whose work overlaps on the GPU (different
-// streams, or different host threads on the same device) race on the array and must be serialised by the caller.
+// up with cudaGetSymbolAddress (with that device current) and caches it.  The cached address belongs to the
+// device's primary context: after a cudaDeviceReset by the host application the entry point must not be called
+// again in that process.  Every call is synchronous -- it reads the tallies back and synchronises its stream before
+// it returns -- so no call can be recorded into a CUDA graph.  All calls share the array and it keeps the last
+// call's contents, so each call clears the counter and tallies before its launch.  Calls whose work overlaps on the
+// GPU (different streams, or different host threads on the same device) race on the array and must be serialised
+// by the caller.
 #include <cuda_runtime.h>
 
 #include <chrono>
