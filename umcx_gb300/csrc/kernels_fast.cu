@@ -10,6 +10,7 @@ template <bool R, bool D>
 static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
     if (lc.rep == kRepWhole) k_forward<false, R, D, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else if (lc.rep == kRepPrefix) k_forward<false, R, D, kRepPrefix><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.rep == kRepOff) k_forward<false, R, D, kRepOff><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else k_forward<false, R, D><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
 }
 
@@ -41,6 +42,7 @@ template <bool R, bool D>
 static cudaError_t allow_big_smem() {
     cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D>);
     if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepPrefix>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepOff>);
     return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, kRepWhole>) : e;
 }
 cudaError_t configure_fast_kernels() {
@@ -83,6 +85,7 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     const bool strict = (s->flags & UMCX_SIM_STRICT_MATH) != 0;
     lc.block = t.block_size > 0 ? t.block_size : 1024;  // one CTA of 32 warps per SM: 2-3 % faster than 256
     lc.aggregate = t.aggregation == 2 ? 1 : 0;
+    lc.rep = s->issavevol ? kRepNone : kRepOff;  // the caller sets the FP64 volume's replication mode
     lc.smem = forward_smem(P, lc.block, lc.savedet);
     while (lc.smem > kMaxDynamicSmem && lc.block > 32) {  // per-lane partial paths of many media: smaller CTAs
         lc.block /= 2;

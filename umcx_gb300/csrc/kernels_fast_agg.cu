@@ -9,6 +9,7 @@ template <bool R, bool D>
 static void launch_agg(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
     if (lc.rep == kRepWhole) k_forward<false, R, D, kRepWhole, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else if (lc.rep == kRepPrefix) k_forward<false, R, D, kRepPrefix, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.rep == kRepOff) k_forward<false, R, D, kRepOff, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else k_forward<false, R, D, kRepNone, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
 }
 
@@ -26,6 +27,7 @@ template <bool R, bool D>
 static cudaError_t allow_big_smem_agg() {
     cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D, kRepNone, true>);
     if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepPrefix, true>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepOff, true>);
     return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, kRepWhole, true>) : e;
 }
 

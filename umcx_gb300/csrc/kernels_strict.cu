@@ -10,6 +10,7 @@ template <bool R, bool D>
 static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
     if (lc.rep == kRepWhole) k_forward<true, R, D, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else if (lc.rep == kRepPrefix) k_forward<true, R, D, kRepPrefix><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.rep == kRepOff) k_forward<true, R, D, kRepOff><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else k_forward<true, R, D><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
 }
 
@@ -17,6 +18,7 @@ template <bool R, bool D>
 static cudaError_t allow_big_smem() {
     cudaError_t e = allow_max_dynamic_smem(k_forward<true, R, D>);
     if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<true, R, D, kRepPrefix>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<true, R, D, kRepOff>);
     return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<true, R, D, kRepWhole>) : e;
 }
 cudaError_t configure_strict_kernels() {

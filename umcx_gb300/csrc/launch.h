@@ -28,7 +28,8 @@ struct LaunchChoice {
     size_t smem = 0;
     bool reflect = false;
     bool savedet = false;
-    int rep = kRepNone;  // replication mode of the FP64 output volume (kRepPrefix / kRepWhole: KParams::rep_mask > 0)
+    int rep = kRepNone;  // replication mode of the FP64 output volume (kRepPrefix / kRepWhole: KParams::rep_mask > 0;
+                         // kRepOff: no output volume)
 };
 
 // buffer extents (elements) for the device bounds checks of a checked build; nothing in production builds

@@ -103,8 +103,9 @@ struct KParams {
 
 // ---------------------------------------------------------------- device bounds checks (checked build variant)
 // Built with UMCX_DEVICE_CHECKS=1 (e.g. UMCX_NVCC_DEFS="UMCX_DEVICE_CHECKS=1"), the kernels test every indexed
-// access of a device buffer -- label reads (and the medium each label names), output deposits, partial-path slots,
-// detected-photon rows and Jacobian adds -- against the buffer's extent first.  An access outside it is skipped and
+// access of a device buffer -- label reads (and the medium each label names), output deposits, detected-photon rows
+// and Jacobian adds -- against the buffer's extent first (partial-path slots are bounded by ppathlen in every
+// build; kSitePath keeps its number for the host's site names).  An access outside it is skipped and
 // recorded in KStats::error as kCheckError + site (the first miss wins); the host turns it into an error naming the
 // site.  Production builds compile none of it.
 #ifndef UMCX_DEVICE_CHECKS
@@ -568,7 +569,9 @@ __device__ __forceinline__ float deposit_value(const PV& P, const Photon& p, con
 // The CTA's copy of the replicated part of an FP64 volume: deposits below `len` go `base` elements further
 // (len = 0: no copy, every deposit goes to the volume itself).  Kernels are instantiated per replication mode:
 // kRepNone, kRepPrefix (the first gates are replicated: one compare per deposit) or kRepWhole (every element is).
-enum { kRepNone = 0, kRepPrefix = 1, kRepWhole = 2 };
+// kRepOff marks a launch that saves no output volume (issavevol 0), so that the forward kernels know at compile time
+// whether a crossing deposits.
+enum { kRepNone = 0, kRepPrefix = 1, kRepWhole = 2, kRepOff = 3 };
 struct Replica {
     unsigned len;
     unsigned base;  // below 2^32: the volume is below 2^31 elements and its copies below 4 Mi elements
@@ -576,7 +579,7 @@ struct Replica {
 template <int REP>
 __device__ __forceinline__ Replica cta_replica(const KParams& P) {
     Replica r{0u, 0u};
-    if (REP != kRepNone) {  // copy c >= 1 of the CTA lies after the volume and copies 1 .. c-1; copy 0 is the volume
+    if (REP == kRepPrefix || REP == kRepWhole) {  // copy c >= 1 of the CTA lies after the volume and copies 1 .. c-1
         const unsigned c = blockIdx.x & P.rep_mask;
         r.len = c ? P.rep_len : 0u;
         r.base = c ? P.dimxyz * static_cast<unsigned>(P.maxgate) + (c - 1u) * P.rep_len : 0u;
@@ -588,6 +591,7 @@ __device__ __forceinline__ Replica cta_replica(const KParams& P) {
 // afterwards), else straight into the FP32 output like the reference (MCX_volume::add, L134-137)
 template <int REP = kRepNone>
 __device__ __forceinline__ void deposit_add(const KBuffers& B, int idx, float v, Replica rep = Replica{0u, 0u}) {
+    if constexpr (REP == kRepOff) return;  // no output volume
     if (!index_ok(&B.stats->error, static_cast<unsigned long long>(static_cast<long long>(idx)), UMCX_EXTENT(B, n_out),
                   kSiteOutput))
         return;
@@ -712,7 +716,8 @@ __device__ __forceinline__ bool start_photon(const PV& P, const LV& labels, Phot
 // (L272-274).  Every kernel (forward, adjoint, replay) advances photons with this one function, so a replayed photon
 // follows the forward pass's trajectory.  RESET_SEGMENT resets the deposit segment at every crossing even when no
 // volume is saved (per-voxel path lengths for the adjoint and the replay); trajectories do not depend on it.
-template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV, class LV>
+// SAVEVOL as for photon_step.
+template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, int SAVEVOL = -1, class PV, class LV>
 __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Medium* sm, Photon& p, Event& ev,
                                         Counters& c, bool active = true) {
     ev.crossed = false;
@@ -743,7 +748,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
             ev.w_before = p.lw;
             ev.gate = deposit_gate(P, p);
             ev.dep_val = deposit_value<STRICT>(P, p, m);
-            if (RESET_SEGMENT || P.issavevol) {
+            if (RESET_SEGMENT || (SAVEVOL < 0 ? P.issavevol != 0 : SAVEVOL != 0)) {
                 p.lw = p.pw;
                 p.lz = 0.f;
             }
@@ -936,11 +941,13 @@ __device__ __forceinline__ bool out_of_budget(const KBuffers& B, unsigned iter, 
 // now, p.lastvox: the voxel left, of medium mid), and after a scatter in medium mid, on_scatter(mid) -- so that
 // nothing a crossing records stays live through the scattering code.  Returns true when the photon ended.
 // RESET_SEGMENT resets the deposit segment at every crossing even when no volume is saved (per-voxel path lengths
-// for the adjoint and the replay); trajectories do not depend on it.  Every kernel advances photons with this
+// for the adjoint and the replay); trajectories do not depend on it.  SAVEVOL as for record_crossing (whether the
+// volume is saved: 1 / 0 known at compile time, -1 read from P).  Every kernel advances photons with this
 // function (the warp-aggregated forward and batched instances with advance(), which performs the same operations
 // in the same order), so a replayed photon follows the forward pass's trajectory.
 // PV is KParams (a single simulation) or SimDesc (a simulation of a batch).
-template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, class PV, class LV, class OnCross, class OnScatter>
+template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, int SAVEVOL = -1, class PV, class LV, class OnCross,
+          class OnScatter>
 __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const Medium* sm, Photon& p, Counters& c,
                                             OnCross&& on_cross, OnScatter&& on_scatter) {
     bool term = false;
@@ -963,7 +970,7 @@ __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const
             const bool late = p.ly > P.tend;
             unsigned newmedia = (newvox >= 0 && !late) ? labels(newvox) : 0u;
             on_cross(mid, m);
-            if (RESET_SEGMENT || P.issavevol) {
+            if (RESET_SEGMENT || (SAVEVOL < 0 ? P.issavevol != 0 : SAVEVOL != 0)) {
                 p.lw = p.pw;
                 p.lz = 0.f;
             }
@@ -1003,15 +1010,17 @@ __device__ __forceinline__ int deposit_gate(const PV& P, const Photon& p) {
 }
 
 // the forward kernels' crossing record: partial path of the medium left (L286-288) and the fluence deposit
-// (L289-291, L359-363) through deposit(voxel, gate, value)
-template <bool STRICT, bool SAVEDET, class PV, class Deposit>
+// (L289-291, L359-363) through deposit(voxel, gate, value).  SAVEVOL: 1 / 0 when the launch is known to save / not
+// to save the output volume, -1 to read P.issavevol.  The partial-path test is one unsigned compare: ppathlen is 0
+// unless partial paths are saved, and label 0 (mid - 1 wraps) has no column.
+template <bool STRICT, bool SAVEDET, int SAVEVOL = -1, class PV, class Deposit>
 __device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, unsigned mid, const Medium& m,
                                                 float* ppath_lane, int* err, Deposit&& deposit) {
+    (void)err;
     if constexpr (SAVEDET) {
-        if ((P.savedetflag & UMCX_DET_PPATH) && mid > 0 && index_ok(err, mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
-            ppath_lane[(mid - 1) * blockDim.x] += p.lz;
+        if (mid - 1u < static_cast<unsigned>(P.ppathlen)) ppath_lane[(mid - 1) * blockDim.x] += p.lz;
     }
-    if (P.issavevol) {
+    if (SAVEVOL < 0 ? P.issavevol != 0 : SAVEVOL != 0) {
         const int gate = deposit_gate(P, p);
         if (gate >= 0) deposit(p.lastvox, gate, deposit_value<STRICT>(P, p, m));
     }
@@ -1055,6 +1064,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
     bool active = false, done = false;
     Counters c;
     const Replica replica = cta_replica<REP>(P);
+    constexpr int SAVEVOL = REP == kRepOff ? 0 : 1;  // kRepOff: the launch saves no output volume
 
     for (unsigned iter = 0;; iter++) {
         if (!active && !done) {  // launch a photon on an idle lane (L761-763)
@@ -1078,20 +1088,19 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
         bool term = false;
         if (AGG) {
             Event ev;
-            advance<STRICT, REFLECT, false>(P, labels, sm, p, ev, c, active);  // no event on an idle lane
-            if (SAVEDET && (P.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0 &&
-                index_ok(&B.stats->error, ev.left_mid - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
+            advance<STRICT, REFLECT, false, SAVEVOL>(P, labels, sm, p, ev, c, active);  // no event on an idle lane
+            if (SAVEDET && ev.crossed && ev.left_mid - 1u < static_cast<unsigned>(P.ppathlen))
                 ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
-            const bool dep = ev.crossed && P.issavevol && ev.gate >= 0;
+            const bool dep = SAVEVOL && ev.crossed && ev.gate >= 0;
             const int dep_idx = dep ? ev.left_vox + ev.gate * static_cast<int>(P.dimxyz) : -1;
             const float dep_val = dep ? ev.dep_val : 0.f;
             deposit_converged<REP>(B, true, aggbuf, tid, lane, dep_idx, dep_val, replica);
             term = ev.term;
         } else if (active) {
-            term = photon_step<STRICT, REFLECT, false>(
+            term = photon_step<STRICT, REFLECT, false, SAVEVOL>(
                 P, labels, sm, p, c,
                 [&](unsigned mid, const Medium& m) {
-                    record_crossing<STRICT, SAVEDET>(P, p, mid, m, ppath + tid, &B.stats->error,
+                    record_crossing<STRICT, SAVEDET, SAVEVOL>(P, p, mid, m, ppath + tid, &B.stats->error,
                                                      [&](int vox, int gate, float v) {
                                                          deposit_add<REP>(B, vox + gate * static_cast<int>(P.dimxyz), v,
                                                                           replica);
@@ -1209,9 +1218,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                 P, labels(), sm, p, c,
                 [&](unsigned m, const Medium& med) {
                     const float seg = p.lz;  // path in the voxel left (the segment is reset at every crossing)
-                    if ((P.savedetflag & UMCX_DET_PPATH) && m > 0 &&
-                        index_ok(&B.stats->error, m - 1u, static_cast<unsigned>(P.ppathlen), kSitePath))
-                        ppath[(m - 1) * bd + tid] += seg;
+                    if (m - 1u < static_cast<unsigned>(P.ppathlen)) ppath[(m - 1) * bd + tid] += seg;
                     float F = 0.f, dF = 0.f;
                     if (P.issavevol) {
                         const int gate = deposit_gate(P, p);
@@ -1497,8 +1504,7 @@ __global__ void __launch_bounds__(1024) k_batch(const BParams BP, const KBuffers
                 const SimDesc& S = sd[sim];
                 const GlobalLabels lab = global_labels(B, S.label_off, S.dimxyz, BP.total_media - S.media_base);
                 advance<false, REFLECT, false>(S, lab, sm + S.media_base, p, ev, c);
-                if (SAVEDET && (S.savedetflag & UMCX_DET_PPATH) && ev.crossed && ev.left_mid > 0 &&
-                    index_ok(&B.stats->error, ev.left_mid - 1u, static_cast<unsigned>(S.ppathlen), kSitePath))
+                if (SAVEDET && ev.crossed && ev.left_mid - 1u < static_cast<unsigned>(S.ppathlen))
                     ppath[(ev.left_mid - 1) * blockDim.x + tid] += ev.seg;  // L286-288
                 const bool dep = ev.crossed && S.issavevol && ev.gate >= 0;
                 dep_idx = dep ? static_cast<long long>(S.out_off) + ev.left_vox +
