@@ -8,7 +8,10 @@ namespace umcx_dev {
 
 template <bool R, bool D>
 static void launch_one(const LaunchChoice& lc, const KParams& P, const KBuffers& B, cudaStream_t st) {
-    if (lc.rep == kRepWhole) k_forward<false, R, D, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    // one-gate volumes (a whole-volume replica or none) take the instances that skip the gate arithmetic
+    if (lc.gate1 && lc.rep == kRepWhole) k_forward<false, R, D, kRepWhole, false, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.gate1 && lc.rep == kRepNone) k_forward<false, R, D, kRepNone, false, true><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
+    else if (lc.rep == kRepWhole) k_forward<false, R, D, kRepWhole><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else if (lc.rep == kRepPrefix) k_forward<false, R, D, kRepPrefix><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else if (lc.rep == kRepOff) k_forward<false, R, D, kRepOff><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
     else k_forward<false, R, D><<<lc.grid, lc.block, lc.smem, st>>>(P, B);
@@ -43,6 +46,8 @@ static cudaError_t allow_big_smem() {
     cudaError_t e = allow_max_dynamic_smem(k_forward<false, R, D>);
     if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepPrefix>);
     if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepOff>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepNone, false, true>);
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(k_forward<false, R, D, kRepWhole, false, true>);
     return e == cudaSuccess ? allow_max_dynamic_smem(k_forward<false, R, D, kRepWhole>) : e;
 }
 cudaError_t configure_fast_kernels() {
@@ -86,6 +91,7 @@ LaunchChoice choose_launch(int device, int sm_count, const umcx_tuning& t, const
     lc.block = t.block_size > 0 ? t.block_size : 1024;  // one CTA of 32 warps per SM: 2-3 % faster than 256
     lc.aggregate = t.aggregation == 2 ? 1 : 0;
     lc.rep = s->issavevol ? kRepNone : kRepOff;  // the caller sets the FP64 volume's replication mode
+    lc.gate1 = s->dim[3] == 1;
     lc.smem = forward_smem(P, lc.block, lc.savedet);
     while (lc.smem > kMaxDynamicSmem && lc.block > 32) {  // per-lane partial paths of many media: smaller CTAs
         lc.block /= 2;

@@ -30,6 +30,7 @@ struct LaunchChoice {
     bool savedet = false;
     int rep = kRepNone;  // replication mode of the FP64 output volume (kRepPrefix / kRepWhole: KParams::rep_mask > 0;
                          // kRepOff: no output volume)
+    bool gate1 = false;  // the output volume has one time gate
 };
 
 // buffer extents (elements) for the device bounds checks of a checked build; nothing in production builds

@@ -1012,8 +1012,10 @@ __device__ __forceinline__ int deposit_gate(const PV& P, const Photon& p) {
 // the forward kernels' crossing record: partial path of the medium left (L286-288) and the fluence deposit
 // (L289-291, L359-363) through deposit(voxel, gate, value).  SAVEVOL: 1 / 0 when the launch is known to save / not
 // to save the output volume, -1 to read P.issavevol.  The partial-path test is one unsigned compare: ppathlen is 0
-// unless partial paths are saved, and label 0 (mid - 1 wraps) has no column.
-template <bool STRICT, bool SAVEDET, int SAVEVOL = -1, class PV, class Deposit>
+// unless partial paths are saved, and label 0 (mid - 1 wraps) has no column.  GATE1: the volume has one time gate,
+// so deposit_gate is 0 exactly when (t - tstart) * rtstep >= 0 and negative otherwise (for every time that is not
+// NaN), which is all the crossing needs to know.
+template <bool STRICT, bool SAVEDET, int SAVEVOL = -1, bool GATE1 = false, class PV, class Deposit>
 __device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, unsigned mid, const Medium& m,
                                                 float* ppath_lane, int* err, Deposit&& deposit) {
     (void)err;
@@ -1021,8 +1023,12 @@ __device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, un
         if (mid - 1u < static_cast<unsigned>(P.ppathlen)) ppath_lane[(mid - 1) * blockDim.x] += p.lz;
     }
     if (SAVEVOL < 0 ? P.issavevol != 0 : SAVEVOL != 0) {
-        const int gate = deposit_gate(P, p);
-        if (gate >= 0) deposit(p.lastvox, gate, deposit_value<STRICT>(P, p, m));
+        if constexpr (GATE1) {
+            if ((p.ly - P.tstart) * P.rtstep >= 0.f) deposit(p.lastvox, 0, deposit_value<STRICT>(P, p, m));
+        } else {
+            const int gate = deposit_gate(P, p);
+            if (gate >= 0) deposit(p.lastvox, gate, deposit_value<STRICT>(P, p, m));
+        }
     }
 }
 
@@ -1037,8 +1043,9 @@ __device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, un
 #define UMCX_FWD_MINB 1
 #endif
 // REP: replication mode of the FP64 output volume (P.rep_mask, P.rep_len; see accumulator_replicas); AGG: fluence
-// deposits aggregated per warp with __match_any_sync (P.aggregate) instead of plain atomics
-template <bool STRICT, bool REFLECT, bool SAVEDET, int REP = kRepNone, bool AGG = false>
+// deposits aggregated per warp with __match_any_sync (P.aggregate) instead of plain atomics; GATE1: the output volume
+// has one time gate (plain-atomic instances)
+template <bool STRICT, bool REFLECT, bool SAVEDET, int REP = kRepNone, bool AGG = false, bool GATE1 = false>
 __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(const KParams P, const KBuffers B) {
     extern __shared__ float4 smem4[];
     // per-lane FP64 energy tallies and launch weight live in shared memory (touched once per photon), which keeps
@@ -1100,7 +1107,7 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
             term = photon_step<STRICT, REFLECT, false, SAVEVOL>(
                 P, labels, sm, p, c,
                 [&](unsigned mid, const Medium& m) {
-                    record_crossing<STRICT, SAVEDET, SAVEVOL>(P, p, mid, m, ppath + tid, &B.stats->error,
+                    record_crossing<STRICT, SAVEDET, SAVEVOL, GATE1>(P, p, mid, m, ppath + tid, &B.stats->error,
                                                      [&](int vox, int gate, float v) {
                                                          deposit_add<REP>(B, vox + gate * static_cast<int>(P.dimxyz), v,
                                                                           replica);
