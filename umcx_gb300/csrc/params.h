@@ -60,6 +60,7 @@ inline KParams make_params(const umcx_sim* s, const float* detpos) {
     P.tstart = s->tstart;
     P.tend = s->tend;
     P.rtstep = s->rtstep;
+    P.gate_off = -(s->tstart * s->rtstep);
     P.unitinmm = s->unitinmm;
     P.isreflect = s->isreflect;
     P.issavevol = s->issavevol;

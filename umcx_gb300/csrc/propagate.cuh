@@ -42,7 +42,6 @@ constexpr float kOneOverC0 = 3.335640951981520e-12f;  // L29
 constexpr float kPi = 3.1415926535897932385f;         // L30
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr unsigned kZeroStepLimit = 255;  // consecutive zero-length steps before a photon is stopped
-constexpr unsigned kStoppedBit = 0x8000u;  // Photon::media bit 15: the photon was stopped by the step cap or guard
 constexpr unsigned kDefaultStepCap = 1u << 24;  // steps of one photon before it is stopped
 
 enum Kind : int { kForward = 0, kAdjoint = 1, kReplay = 2 };
@@ -98,6 +97,7 @@ struct KParams {
     unsigned long long budget_ns;  // wall-clock budget of the launch (checked against %globaltimer)
     unsigned rep_mask;             // forward kernel: CTA b deposits into copy c = b & rep_mask of the first rep_len
     unsigned rep_len;              // elements of the FP64 volume (copy 0 is the volume itself; see accumulator_replicas)
+    float gate_off;                // -tstart * rtstep: the fast kernels' time gate is t * rtstep + gate_off
     float4 det[UMCX_MAX_DET];
 };
 
@@ -168,21 +168,27 @@ __device__ __forceinline__ void rng_reseed(Rng& r, unsigned s0, unsigned s1, uns
     r.t1 = (static_cast<unsigned long long>(s2) << 32) | s3;
 }
 
-__device__ __forceinline__ float rng_rand01(Rng& r) {
+// one xorshift128+ draw as the float 1 + (23 random bits) / 2^23 in [1, 2); rng_rand01 subtracts the 1 (exactly)
+__device__ __forceinline__ float rng_rand12(Rng& r) {
     unsigned long long a = r.t0;
     const unsigned long long b = r.t1;
     r.t0 = b;
     a ^= a << 23;
     r.t1 = a ^ b ^ (a >> 18) ^ (b >> 5);
     const unsigned lo = static_cast<unsigned>(r.t1 + b);
-    return __uint_as_float(0x3F800000u | (lo >> 9)) - 1.0f;
+    return __uint_as_float(0x3F800000u | (lo >> 9));
 }
+
+__device__ __forceinline__ float rng_rand01(Rng& r) { return rng_rand12(r) - 1.0f; }
 
 template <bool STRICT>
 __device__ __forceinline__ float scat_len(Rng& r) {  // L212-214
-    const float u = rng_rand01(r) + FLT_EPSILON;
-    if constexpr (STRICT) return -logf(u);
-    else return -__logf(u);
+    if constexpr (STRICT) {
+        return -logf(rng_rand01(r) + FLT_EPSILON);
+    } else {
+        // (f - 1) + 2^-23 and f + (2^-23 - 1) are both exact for f = 1 + k 2^-23 (k < 2^23): one addition instead of two
+        return -__logf(rng_rand12(r) + (FLT_EPSILON - 1.0f));
+    }
 }
 
 template <bool STRICT>
@@ -414,7 +420,10 @@ __device__ __forceinline__ int step(const PV& P, Photon& p, const Medium& m, boo
         p.lx -= used;
         p.ly += dist * m.a.w * kOneOverC0;
     } else {
-        dist = (mus == 0.f) ? dist : (used * m.b.x);
+        // a crossing step moves the wall distance itself (the reference's used / mus is that distance rounded
+        // twice; with mus = 0 it is the only choice); otherwise the free path used / mus.  A free path of 0 (a draw
+        // of -log(1)) therefore moves nothing, which lets photon_step run the step without testing lx > 0 first.
+        dist = *crossed ? dist : used * m.b.x;
         const float2 pxy = __ffma2_rn(make_float2(dist, dist), make_float2(p.vx, p.vy), make_float2(p.px, p.py));
         p.px = pxy.x;
         p.py = pxy.y;
@@ -439,7 +448,12 @@ template <bool STRICT>
 __device__ __forceinline__ void scatter(Photon& p, const Medium& m) {
     p.lx = scat_len<STRICT>(p.rng);
     float sphi, cphi, stheta, ctheta;
-    sincos_<STRICT>((2.f * kPi) * rng_rand01(p.rng), &sphi, &cphi);
+    if constexpr (STRICT) {
+        sincos_<STRICT>((2.f * kPi) * rng_rand01(p.rng), &sphi, &cphi);
+    } else {
+        // 2 pi (f - 1) with f - 1 exact, as one fused multiply-add with the same single rounding
+        sincos_<STRICT>(fmaf(rng_rand12(p.rng), 2.f * kPi, -2.f * kPi), &sphi, &cphi);
+    }
     const float g = m.a.z;
     if constexpr (STRICT) {
         float th;
@@ -613,6 +627,10 @@ __global__ void k_fp64_to_fp32(const double* __restrict__ src, float* __restrict
                                unsigned reps, unsigned long long len);
 
 // =============================================================================================== loop building blocks
+// Per-lane event counts.  The fast kernels do not count scatters one by one: there every voxel step either crosses
+// a voxel boundary, uses up the free path (and the photon scatters) or stops the photon (step cap, zero-progress
+// guard), so the scatters are steps - crossings - stopped photons (flush_tallies and rare_flush).  The strict kernels
+// skip the step when the free path is 0, as the reference does (L283), so they count scatters in `scat`.
 struct Counters {
     unsigned steps = 0, cross = 0, scat = 0;
 };
@@ -685,9 +703,10 @@ __device__ __forceinline__ GlobalLabels global_labels(const KBuffers& B, unsigne
     return g;
 }
 
-// the kernels call this where a photon ends: photons stopped by the step cap or the zero-progress guard
+// the kernels call this where a photon ends: photons stopped by the step cap or the zero-progress guard (a photon
+// that reaches either limit ends at that step, so the test here finds exactly those)
 __device__ __forceinline__ void count_stopped(const Photon& p) {
-    if (p.media & kStoppedBit) rare_count(kRareCap);
+    if (p.nsteps > kDefaultStepCap || p.media >= (kZeroStepLimit << 16)) rare_count(kRareCap);
 }
 
 // Boundary reflection switch of one simulation.  A single-simulation kernel is instantiated with REFLECT equal to
@@ -695,6 +714,9 @@ __device__ __forceinline__ void count_stopped(const Photon& p) {
 __device__ __forceinline__ bool reflect_on(const KParams&) { return true; }
 template <class PV>
 __device__ __forceinline__ bool reflect_on(const PV& S) { return S.isreflect != 0; }
+
+template <bool STRICT, class PV>
+__device__ __forceinline__ int deposit_gate(const PV& P, const Photon& p);  // (below)
 
 // L761-762 + L262-271: seed photon idx, launch it, move it onto the grid; false when it misses the grid
 template <bool STRICT, class PV, class LV>
@@ -723,7 +745,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
     ev.crossed = false;
     ev.term = false;
     ev.scattered = false;
-    if (active && p.lx > 0.f) {
+    if (active && (!STRICT || p.lx > 0.f)) {  // a fast step with lx = 0 moves nothing (as in photon_step)
         const unsigned mid = p.media & UMCX_LABEL_MASK;
         const Medium m = sm[mid];
         bool crossed;
@@ -736,8 +758,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
         // `media` and stop the photon after kZeroStepLimit of them, like the step cap
         if (moved == 0.f) p.media += 0x10000u;
         else p.media &= 0xFFFFu;
-        const bool capped = ++p.nsteps > kDefaultStepCap || p.media >= (kZeroStepLimit << 16);
-        p.media |= capped ? kStoppedBit : 0u;  // counted where the photon ends (count_stopped)
+        const bool capped = ++p.nsteps > kDefaultStepCap || p.media >= (kZeroStepLimit << 16);  // (count_stopped)
         ev.term = capped;
         if (!capped && newvox != p.lastvox) {
             c.cross++;
@@ -746,7 +767,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
             ev.left_mid = mid;
             ev.seg = p.lz;
             ev.w_before = p.lw;
-            ev.gate = deposit_gate(P, p);
+            ev.gate = deposit_gate<STRICT>(P, p);
             ev.dep_val = deposit_value<STRICT>(P, p, m);
             if (RESET_SEGMENT || (SAVEVOL < 0 ? P.issavevol != 0 : SAVEVOL != 0)) {
                 p.lw = p.pw;
@@ -779,7 +800,7 @@ __device__ __forceinline__ void advance(const PV& P, const LV& labels, const Med
         ev.scattered = true;
         ev.scat_mid = p.media & UMCX_LABEL_MASK;
         scatter<STRICT>(p, sm[ev.scat_mid]);
-        c.scat++;
+        if (STRICT) c.scat++;
     }
 }
 
@@ -886,30 +907,38 @@ __device__ __forceinline__ void write_detp(const PV& P, const KBuffers& B, const
 }
 
 // per-warp reduction of the lane tallies, one set of atomics per warp
+template <bool STRICT = false>
 __device__ __forceinline__ void flush_tallies(const KBuffers& B, unsigned lane, double tot, double esc, Counters c) {
     for (int off = 16; off > 0; off >>= 1) {
         tot += __shfl_down_sync(kFull, tot, off);
         esc += __shfl_down_sync(kFull, esc, off);
         c.steps += __shfl_down_sync(kFull, c.steps, off);
         c.cross += __shfl_down_sync(kFull, c.cross, off);
-        c.scat += __shfl_down_sync(kFull, c.scat, off);
+        if (STRICT) c.scat += __shfl_down_sync(kFull, c.scat, off);
     }
     if (lane == 0) {
         atomicAdd(&B.stats->total, tot);
         atomicAdd(&B.stats->escape, esc);
         atomicAdd(&B.stats->steps, static_cast<unsigned long long>(c.steps));
         atomicAdd(&B.stats->crossings, static_cast<unsigned long long>(c.cross));
-        atomicAdd(&B.stats->scatters, static_cast<unsigned long long>(c.scat));
+        // fast kernels: steps - crossings (the CTA's stopped photons are taken off in rare_flush); modulo 2^64, so the
+        // total is exact whenever every photon ended (a launch stopped by its wall-clock budget reports partial counts)
+        atomicAdd(&B.stats->scatters, STRICT ? static_cast<unsigned long long>(c.scat)
+                                             : static_cast<unsigned long long>(c.steps) - c.cross);
     }
 }
 
 // the CTA's rare-event counts into the launch statistics; every thread of the CTA must call it
+template <bool STRICT = false>
 __device__ __forceinline__ void rare_flush(const KBuffers& B) {
     __syncthreads();
     if (threadIdx.x == 0) {
         atomicAdd(&B.stats->launched, s_rare[kRareLaunch]);
         atomicAdd(&B.stats->reflections, s_rare[kRareRefl]);
-        if (s_rare[kRareCap]) atomicAdd(&B.stats->capped, s_rare[kRareCap]);
+        if (s_rare[kRareCap]) {
+            atomicAdd(&B.stats->capped, s_rare[kRareCap]);
+            if (!STRICT) atomicAdd(&B.stats->scatters, 0ULL - s_rare[kRareCap]);  // its last step did not scatter
+        }
     }
 }
 
@@ -951,7 +980,9 @@ template <bool STRICT, bool REFLECT, bool RESET_SEGMENT, int SAVEVOL = -1, class
 __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const Medium* sm, Photon& p, Counters& c,
                                             OnCross&& on_cross, OnScatter&& on_scatter) {
     bool term = false;
-    if (p.lx > 0.f) {
+    // the reference steps only while lx > 0 (L283); a fast step with lx = 0 moves nothing and does not cross, so the
+    // fast kernels skip the test (the scatter below follows in both cases; only the step count differs)
+    if (!STRICT || p.lx > 0.f) {
         const unsigned mid = p.media & UMCX_LABEL_MASK;
         const Medium m = sm[mid];
         bool crossed;
@@ -962,7 +993,6 @@ __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const
         if (moved == 0.f) p.media += 0x10000u;
         else p.media &= 0xFFFFu;
         const bool capped = ++p.nsteps > kDefaultStepCap || p.media >= (kZeroStepLimit << 16);
-        p.media |= capped ? kStoppedBit : 0u;
         term = capped;
         if (!capped && newvox != p.lastvox) {
             c.cross++;
@@ -995,18 +1025,31 @@ __device__ __forceinline__ bool photon_step(const PV& P, const LV& labels, const
     if (!term && p.lx <= 0.f) {
         const unsigned mid = p.media & UMCX_LABEL_MASK;
         scatter<STRICT>(p, sm[mid]);
-        c.scat++;
+        if (STRICT) c.scat++;
         on_scatter(mid);
     }
     return term;
 }
 
+// x = (t - tstart) * rtstep, the position of time t in the gates (L290).  The fast kernels of a single simulation
+// compute it as one fused multiply-add t * rtstep + gate_off (gate_off = -tstart * rtstep), identical when tstart is
+// 0 and within a rounding of it otherwise; the strict kernels and a batch's simulations use the reference's form.
+template <bool STRICT, class PV>
+__device__ __forceinline__ float gate_pos(const PV& P, float t) {
+    return (t - P.tstart) * P.rtstep;
+}
+template <bool STRICT>
+__device__ __forceinline__ float gate_pos(const KParams& P, float t) {
+    if constexpr (STRICT) return (t - P.tstart) * P.rtstep;
+    else return fmaf(t, P.rtstep, P.gate_off);
+}
+
 // the time gate of a deposit at the photon's current time: (int)fminf(maxgate - 1, floorf(x)) as one rounding
 // conversion and an integer min (same value for every x: the conversion saturates like the reference's cast chain
 // does on the device); negative before tstart
-template <class PV>
+template <bool STRICT, class PV>
 __device__ __forceinline__ int deposit_gate(const PV& P, const Photon& p) {
-    return min(__float2int_rd((p.ly - P.tstart) * P.rtstep), P.maxgate - 1);
+    return min(__float2int_rd(gate_pos<STRICT>(P, p.ly)), P.maxgate - 1);
 }
 
 // the forward kernels' crossing record: partial path of the medium left (L286-288) and the fluence deposit
@@ -1024,9 +1067,9 @@ __device__ __forceinline__ void record_crossing(const PV& P, const Photon& p, un
     }
     if (SAVEVOL < 0 ? P.issavevol != 0 : SAVEVOL != 0) {
         if constexpr (GATE1) {
-            if ((p.ly - P.tstart) * P.rtstep >= 0.f) deposit(p.lastvox, 0, deposit_value<STRICT>(P, p, m));
+            if (gate_pos<STRICT>(P, p.ly) >= 0.f) deposit(p.lastvox, 0, deposit_value<STRICT>(P, p, m));
         } else {
-            const int gate = deposit_gate(P, p);
+            const int gate = deposit_gate<STRICT>(P, p);
             if (gate >= 0) deposit(p.lastvox, gate, deposit_value<STRICT>(P, p, m));
         }
     }
@@ -1131,8 +1174,8 @@ __global__ void __launch_bounds__(UMCX_FWD_THREADS, UMCX_FWD_MINB) k_forward(con
             active = false;
         }
     }
-    flush_tallies(B, lane, tally[tid], tally[blockDim.x + tid], c);
-    rare_flush(B);
+    flush_tallies<STRICT>(B, lane, tally[tid], tally[blockDim.x + tid], c);
+    rare_flush<STRICT>(B);
 }
 
 // =============================================================================================== adjoint kernel
@@ -1228,7 +1271,7 @@ __global__ void __launch_bounds__(1024) k_adjoint(const KParams P, const KBuffer
                     if (m - 1u < static_cast<unsigned>(P.ppathlen)) ppath[(m - 1) * bd + tid] += seg;
                     float F = 0.f, dF = 0.f;
                     if (P.issavevol) {
-                        const int gate = deposit_gate(P, p);
+                        const int gate = deposit_gate<false>(P, p);
                         if (gate >= 0) {
                             F = deposit_value<false>(P, p, med);
                             deposit_add<REP>(B, p.lastvox + gate * static_cast<int>(P.dimxyz), F, replica);
