@@ -54,21 +54,21 @@ METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates
 # that photon count.  None where no capture exists; the line then reports null for those fractions.
 FORWARD = {
     "c2": {"json": CONFIG, "photons": 10000000, "workload": WORKLOAD,
-           # profiles/k_forward_workloads.md: 3.9196e10 warp instructions / 3.4361e9 steps; 93.3 MB + 3.066 GB
-           "warp_inst_per_step": 11.41, "dram_bytes": 93263104 + 3066302464},
+           # profiles/k_forward_workloads.md: 3.7621e10 warp instructions / 3.4359e9 steps; 93.3 MB + 3.067 GB
+           "warp_inst_per_step": 10.95, "dram_bytes": 93273856 + 3066618368},
     "c1": {"json": config1(), "photons": 1000000, "steps": 20,
            "workload": "homogeneous 60^3 cube, pencil beam, one 5 ns gate, no reflection (configuration 1)",
-           # 4.1648e9 / 1.9618e8 steps (at 1e6 photons the launch's drain is a large share); 13.9 MB read
-           "warp_inst_per_step": 21.23, "dram_bytes": 13947136},
+           # 3.8749e9 / 1.9618e8 steps (at 1e6 photons the launch's drain is a large share); 13.9 MB read
+           "warp_inst_per_step": 19.75, "dram_bytes": 13941504},
     "cube60": {"args": ["--bench", "cube60"], "photons": 100000000, "steps": 5,
                "workload": "the reference's cube60 benchmark: configuration 1 plus four saved detectors, 1e8 photons "
                            "(published: 175 075 photons/ms on an RTX 5090)",
-               # 1.8144e11 / 1.9626e10 steps; 14.4 MB read (the 1.7 MB FP64 volume stays in L2)
-               "warp_inst_per_step": 9.245, "dram_bytes": 14393344 + 1792},
+               # 1.7139e11 / 1.9626e10 steps; 14.2 MB read (the 1.7 MB FP64 volume stays in L2)
+               "warp_inst_per_step": 8.733, "dram_bytes": 14177536 + 2304},
     "c3": {"json": config3(), "photons": 100000000, "steps": 5,
            "workload": "200^3 layered domain of 0.005 mm voxels with a cylinder, disk source, 1 ns gate (configuration 3)",
-           # 2.8430e11 / 2.9111e10 steps; 69.4 MB read + 10.9 GB of FP64 accumulator lines written back
-           "warp_inst_per_step": 9.766, "dram_bytes": 69396736 + 10901503744},
+           # 2.6523e11 / 2.9111e10 steps; 69.4 MB read + 10.9 GB of FP64 accumulator lines written back
+           "warp_inst_per_step": 9.111, "dram_bytes": 69378560 + 10894940160},
 }
 
 # per-event FP32 and SFU-class operation counts (FMA = 1 op), fixed from the reference's formulas:
