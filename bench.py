@@ -29,13 +29,13 @@ the same configuration.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from pathlib import Path
 
@@ -54,17 +54,17 @@ METRIC = "photons/ms (forward, heterogeneous 60^3 + sphere, reflection, 50 gates
 # that photon count.  None where no capture exists; the line then reports null for those fractions.
 FORWARD = {
     "c2": {"json": CONFIG, "photons": 10000000, "workload": WORKLOAD,
-           # profiles/k_forward_workloads.md: 3.7621e10 warp instructions / 3.4359e9 steps; 93.3 MB + 3.067 GB
-           "warp_inst_per_step": 10.95, "dram_bytes": 93273856 + 3066618368},
+           # profiles/k_forward_workloads.md: 3.7381e10 warp instructions / 3.4359e9 steps; 93.3 MB + 3.065 GB
+           "warp_inst_per_step": 10.88, "dram_bytes": 93255680 + 3065493760},
     "c1": {"json": config1(), "photons": 1000000, "steps": 20,
            "workload": "homogeneous 60^3 cube, pencil beam, one 5 ns gate, no reflection (configuration 1)",
-           # 3.8749e9 / 1.9618e8 steps (at 1e6 photons the launch's drain is a large share); 13.9 MB read
-           "warp_inst_per_step": 19.75, "dram_bytes": 13941504},
+           # 3.8693e9 / 1.9618e8 steps (at 1e6 photons the launch's drain is a large share); 13.9 MB read
+           "warp_inst_per_step": 19.72, "dram_bytes": 13939968},
     "cube60": {"args": ["--bench", "cube60"], "photons": 100000000, "steps": 5,
                "workload": "the reference's cube60 benchmark: configuration 1 plus four saved detectors, 1e8 photons "
                            "(published: 175 075 photons/ms on an RTX 5090)",
-               # 1.7139e11 / 1.9626e10 steps; 14.2 MB read (the 1.7 MB FP64 volume stays in L2)
-               "warp_inst_per_step": 8.733, "dram_bytes": 14177536 + 2304},
+               # 1.7139e11 / 1.9626e10 steps; 14.1 MB read (the 1.7 MB FP64 volume stays in L2)
+               "warp_inst_per_step": 8.733, "dram_bytes": 14073856 + 1536},
     "c3": {"json": config3(), "photons": 100000000, "steps": 5,
            "workload": "200^3 layered domain of 0.005 mm voxels with a cylinder, disk source, 1 ns gate (configuration 3)",
            # 2.6523e11 / 2.9111e10 steps; 69.4 MB read + 10.9 GB of FP64 accumulator lines written back
@@ -85,7 +85,9 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region.  nvidia-smi writes its samples straight into a
+    temporary file (no reader thread in this process, so sampling never competes with the timed loop for the
+    interpreter)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -95,21 +97,16 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines = []
-        self.thread = None
+        self.out = None
 
     def start(self):
         try:
+            self.out = tempfile.TemporaryFile(mode="w+")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
+                                         stdout=self.out, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
 
     def stop(self) -> dict:
         if self.proc is None:
@@ -119,8 +116,9 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        if self.thread:
-            self.thread.join(timeout=2)
+        self.out.seek(0)
+        self.lines = [ln.strip() for ln in self.out]
+        self.out.close()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -268,6 +266,7 @@ def time_forward(ctx, job, photons: int, steps: int, warmup: int, device: int, f
     if shard is not None:
         shard.barrier()
     torch.cuda.synchronize()
+    gc.disable()  # no collector pause between a step's start event and its launches
     for _ in range(steps):
         flush.fill_(1)
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -282,6 +281,7 @@ def time_forward(ctx, job, photons: int, steps: int, warmup: int, device: int, f
         step_ms.append(ev0.elapsed_time(ev1))
         kernel_ms.append(r.kernel_ms)
         results.append(r)
+    gc.enable()
     if shard is not None:
         shard.barrier()
     torch.cuda.synchronize()

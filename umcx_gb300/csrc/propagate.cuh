@@ -595,7 +595,10 @@ __device__ __forceinline__ Replica cta_replica(const KParams& P) {
     Replica r{0u, 0u};
     if (REP == kRepPrefix || REP == kRepWhole) {  // copy c >= 1 of the CTA lies after the volume and copies 1 .. c-1
         const unsigned c = blockIdx.x & P.rep_mask;
-        r.len = c ? P.rep_len : 0u;
+        // copy 0 is the volume itself (base 0), so every CTA can compare with the kernel parameter: the length is
+        // then read from the constant bank and the loop keeps one register (base) for the replica (-1.1 % at
+        // configuration 2)
+        r.len = P.rep_len;
         r.base = c ? P.dimxyz * static_cast<unsigned>(P.maxgate) + (c - 1u) * P.rep_len : 0u;
     }
     return r;
