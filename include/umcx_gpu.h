@@ -98,11 +98,13 @@ typedef struct umcx_result {
     uint64_t detected;        /* MCX_detect::detectedphoton: all detections, including those beyond maxdetphotons */
     uint64_t saved;           /* MCX_detect::savedcount() */
     uint64_t launched;        /* photons processed */
-    uint64_t steps;           /* voxel steps (MCX_photon::step calls) */
+    uint64_t steps;           /* voxel steps (MCX_photon::step calls; the fast kernels also count a step of length 0
+                                 after a free-path draw of exactly 0, where the reference scatters without a step) */
     uint64_t crossings;       /* voxel changes (deposit sites) */
     uint64_t scatters;        /* scattering events */
     uint64_t reflections;     /* MCX_photon::reflect calls */
-    uint64_t capped;          /* photons terminated by the per-photon step cap (0 in a normal run) */
+    uint64_t capped;          /* photons stopped by the per-photon step cap or the zero-progress guard (0 in a
+                                 normal run) */
     float kernel_ms;          /* device time of the propagation kernel (CUDA events) */
     float total_ms;           /* wall time of the whole call */
     int32_t status;           /* same as the return value */
