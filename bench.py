@@ -267,6 +267,22 @@ def time_forward(ctx, job, photons: int, steps: int, warmup: int, device: int, f
         shard.barrier()
     torch.cuda.synchronize()
     gc.disable()  # no collector pause between a step's start event and its launches
+    try:
+        _timed_steps(ctx, job, sim, d_lab, d_flu, d_det, stream, flush, shard, steps, step_ms, kernel_ms, results)
+    finally:
+        gc.enable()
+    if shard is not None:
+        shard.barrier()
+    torch.cuda.synchronize()
+    return step_ms, kernel_ms, results
+
+
+def _timed_steps(ctx, job, sim, d_lab, d_flu, d_det, stream, flush, shard, steps, step_ms, kernel_ms, results):
+    """The timed steps of time_forward: each bracketed by CUDA events on the launching stream."""
+    import torch
+
+    from umcx_gb300 import detp_columns
+
     for _ in range(steps):
         flush.fill_(1)
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -281,11 +297,6 @@ def time_forward(ctx, job, photons: int, steps: int, warmup: int, device: int, f
         step_ms.append(ev0.elapsed_time(ev1))
         kernel_ms.append(r.kernel_ms)
         results.append(r)
-    gc.enable()
-    if shard is not None:
-        shard.barrier()
-    torch.cuda.synchronize()
-    return step_ms, kernel_ms, results
 
 
 def time_e2e(ctx, job, photons: int, reps: int, flush) -> dict:

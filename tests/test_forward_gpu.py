@@ -68,12 +68,21 @@ def with_output(spec, otype):
     return cfg
 
 
+def with_window(spec, t0, t1, dt):
+    """The same simulation with another time window: with t0 > 0 the deposits of the first nanoseconds fall before
+    the first gate and are skipped by both sides (the reference writes them before its array)."""
+    cfg = json.loads(json.dumps(spec))
+    cfg["Forward"] = {"T0": t0, "T1": t1, "Dt": dt}
+    return cfg
+
+
 CASES = {
     "c1": (C1, 1000000, 20),
     "c2": (C2, 10000000, 20),
     "c3": (C3, 10000000, 10),
     "c1_fluence": (with_output(C1, "f"), 1000000, 20),
     "c2_fluence": (with_output(C2, "f"), 1000000, 20),
+    "c2_late_window": (with_window(C2, 1e-9, 5e-9, 1e-10), 1000000, 20),
     "cube60b": (["--bench", "cube60b"], 200000, 20),
     "spherebox": (["--bench", "spherebox"], 100000, 20),
     "sphshells": (["--bench", "sphshells"], 50000, 10),
