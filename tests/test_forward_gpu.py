@@ -142,6 +142,47 @@ def test_forward_parity(ctx, name):
     print(line)
 
 
+def test_detected_exit_records_match_oracle(ctx):
+    """Detected-photon rows with every SaveDetFlag column -- detector id, partial paths, exit position and exit
+    direction (MCX_photon::savedetector, src/umcx.cpp:429-435; row layout L171-174): per detector the count and the
+    mean of every partial-path, position and direction column agree with the oracle within 3 standard errors, or to
+    within 1e-5 (voxel units, direction components) for a column without spread -- the exit coordinate of the z = 0
+    face, which both sides reach within a float rounding of 0; every exit point lies within its detector's radius (the
+    detection test, L430-431) and every exit direction is a unit vector leaving through the z = 0 face that holds the
+    detectors."""
+    cfg = json.loads(json.dumps(C2))
+    cfg["Session"]["SaveDetFlag"] = 1 + 4 + 16 + 32
+    job = job_for(cfg, 1000000)
+    sim = job.sim
+    g = run_batches(gpu_runner(ctx, job), sim, 20)
+    c = run_batches(cpu_runner(job), sim, 20)
+    k = sim.mediumnum
+    groups = {"partial path": slice(1, 1 + k), "exit position": slice(1 + k, 4 + k),
+              "exit direction": slice(4 + k, 7 + k)}
+    line = "exit records:"
+    for name, cols in groups.items():
+        zmax = 0.0
+        for d, ((n1, m1, s1), (n2, m2, s2)) in enumerate(zip(det_stats(g.detp, sim.detnum, cols),
+                                                             det_stats(c.detp, sim.detnum, cols))):
+            zn = (n1 - n2) / math.sqrt(n1 + n2) if n1 + n2 else 0.0
+            assert abs(zn) < 3, (name, d, n1, n2)
+            if n1 > 30 and n2 > 30:
+                z = (m1 - m2) / np.sqrt(s1 ** 2 + s2 ** 2 + 1e-30)
+                keep = np.isfinite(z) & (np.abs(m1 - m2) >= 1e-5)  # a spread-free column only has to agree to 1e-5
+                assert np.all(np.abs(z[keep]) < 3), (name, d, m1, m2, z)
+                zmax = max(zmax, float(np.abs(z[keep]).max()) if keep.any() else 0.0)
+        line += f" {name} max |z| {zmax:.2f};"
+    rows = np.concatenate([r for r in g.detp if r is not None and len(r)], axis=0)
+    assert rows.shape[1] == 7 + k and len(rows) > 1000
+    det = np.asarray(job.detpos, dtype=np.float64).reshape(-1, 4)
+    centre = det[rows[:, 0].astype(int) - 1]
+    dist = np.linalg.norm(rows[:, 1 + k:4 + k] - centre[:, :3], axis=1)
+    assert np.all(dist < centre[:, 3] + 1e-4), dist.max()
+    v = rows[:, 4 + k:7 + k]
+    assert np.all(np.abs(np.linalg.norm(v, axis=1) - 1.0) < 1e-4) and np.all(v[:, 2] < 0.0)
+    print(line + f" {len(rows)} rows, largest distance to the detector centre {dist.max():.3f} (radius 1)")
+
+
 @pytest.mark.parametrize("name,spec,photons", [
     ("c1", C1, 10000000),    # configuration 1 geometry at 10x its photon count
     ("c2", C2, 1000000),
