@@ -95,6 +95,11 @@ CASES = {
                  '{"Optode":{"Source":{"Type":"fourier","Param1":[40,0,0,2.25],"Param2":[0,40,0,1.5]}}}'],
                 100000, 20),
     "shapes": (SHAPES, 50000, 10),
+    # sources outside the grid: every photon is moved onto it first (MCX_photon::skip, L339-358, weight reset to 1),
+    # and most of the wide cone's photons miss it (counted as launched, nothing else, L263-266)
+    "outside_pencil": (["--bench", "cube60", "--json", '{"Optode":{"Source":{"Pos":[29.5,29.5,-10]}}}'], 100000, 20),
+    "outside_cone": (["--bench", "cube60", "--json",
+                      '{"Optode":{"Source":{"Type":"cone","Pos":[29.5,29.5,-20],"Param1":[0.9,0,0,0]}}}'], 200000, 20),
 }
 
 
