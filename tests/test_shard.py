@@ -116,9 +116,9 @@ def test_two_ranks_torch_tensors_equal_single_run(tmp_path):
     assert list(got["mx"]) == [1.0, 10.0]
 
 
-def _worker_gpu(rank, world, port, outdir):
-    """Each rank runs its photon range through the CUDA library on cuda:0, then the ranks reduce (gloo; the two
-    processes share one GPU, and no kernel of one waits for the other: the exchange is on the host)."""
+def _worker_gpu(rank, world, port, outdir, backend="gloo"):
+    """Each rank runs its photon range through the CUDA library on cuda:0, then the ranks reduce (gloo when two
+    processes share one GPU: no kernel of one waits for the other, the exchange is on the host; nccl with one rank)."""
     sys.path.insert(0, str(ROOT))
     import torch
 
@@ -126,7 +126,7 @@ def _worker_gpu(rank, world, port, outdir):
     from umcx_gb300.shard import Shard, shard_sim
 
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
-    sh = Shard.init("gloo")
+    sh = Shard.init(backend)
     job = Job.from_args(["--bench", "cubesph60b", "-n", "200000"])
     s = shard_sim(job.sim, rank, world)
     torch.cuda.set_device(0)
@@ -137,10 +137,13 @@ def _worker_gpu(rank, world, port, outdir):
         d_det = torch.zeros(s.maxdetphotons * cols, dtype=torch.float32, device="cuda")
         r = ctx.forward_device(s, d_lab, job.media, job.detpos, d_flu, d_det, torch.cuda.current_stream())
         out = sh.reduce_device(d_flu, d_det[: r.saved * cols].view(-1, cols), r)
+        out["max_ms"] = sh.max_over_ranks([r.kernel_ms])[0]
+        sh.barrier()
         if rank == 0:
             np.savez(os.path.join(outdir, "gpu.npz"), f=d_flu.cpu().numpy(), esc=out["energy_escape"],
                      tot=out["energy_total"], rows=out["rows"].cpu().numpy(), launched=out["launched"],
-                     steps=out["steps"], crossings=out["crossings"], detected=out["detected"])
+                     steps=out["steps"], crossings=out["crossings"], detected=out["detected"], max_ms=out["max_ms"],
+                     kernel_ms=r.kernel_ms)
     sh.close()
 
 
@@ -165,5 +168,33 @@ def test_two_ranks_on_the_cuda_path_equal_single_run(tmp_path):
     assert abs(float(got["tot"]) - r.energy_total) <= 1e-9 * r.energy_total
     assert abs(float(got["esc"]) - r.energy_escape) <= 1e-9 * r.energy_total
     np.testing.assert_allclose(got["f"], one.fluence.ravel(), rtol=2e-5, atol=1e-6)
+    a, b = got["rows"], one.detp
+    np.testing.assert_array_equal(a[np.lexsort(a.T[::-1])], b[np.lexsort(b.T[::-1])])
+
+
+@pytest.mark.gpu
+def test_one_nccl_rank_on_the_cuda_path_equals_single_run(tmp_path):
+    """The reduction that bench.py --gpus N performs under NCCL (in-place all-reduce of the device volume, all-gather
+    of the detected rows with padded counts, tallies and the max over ranks), run by one NCCL rank on the device
+    tensors of its own run (one GPU cannot hold two NCCL ranks): counts and detected rows equal the single run, energies
+    and the volume to their summation order."""
+    import torch.multiprocessing as mp
+
+    from umcx_gb300 import Context, Job
+
+    port = _free_port()
+    mp.start_processes(_worker_gpu, args=(1, port, str(tmp_path), "nccl"), nprocs=1, start_method="spawn", join=True)
+    got = np.load(tmp_path / "gpu.npz")
+    job = Job.from_args(["--bench", "cubesph60b", "-n", "200000"])
+    with Context(0) as ctx:
+        one = ctx.forward(job.sim, job.labels, job.media, job.detpos)
+    r = one.result
+    assert (int(got["launched"]), int(got["steps"]), int(got["crossings"]), int(got["detected"])) == (
+        r.launched, r.steps, r.crossings, r.detected)
+    # (the FP64 tallies are sums of per-warp atomics: their order, and so their last bits, varies between runs)
+    assert abs(float(got["tot"]) - r.energy_total) <= 1e-12 * r.energy_total
+    assert abs(float(got["esc"]) - r.energy_escape) <= 1e-12 * r.energy_total
+    assert float(got["max_ms"]) == float(got["kernel_ms"])
+    np.testing.assert_allclose(got["f"], one.fluence.ravel(), rtol=2e-6, atol=1e-7)
     a, b = got["rows"], one.detp
     np.testing.assert_array_equal(a[np.lexsort(a.T[::-1])], b[np.lexsort(b.T[::-1])])
